@@ -1,0 +1,424 @@
+#!/usr/bin/env python3
+"""Benchmark: sRGBA8 mip-chain generation on GB300 through the C ABI.
+
+Headline workload: one 16384x16384 sRGBA8 image of uniform random bytes,
+full 15-level chain (the reference's per-dispatch schedule F6 F6 F2), inputs
+resident in HBM.  A step is one full chain.  value = microseconds per chain
+for the whole job (lower is better).  The base level (1 GiB) is larger than
+L2, so no flush is needed between steps of the headline loop.
+
+Also reported (key "extra"): 4096^2, 4095^2, 4094^2, 1920x1080 and 2048^2
+chains, L2-flushed and warm; the roofline of the dominant kernel; the CPU
+baseline (a port of the reference's cpuGenerateMipmaps_sRGBA); an end-to-end
+number with host buffers (H2D copy of the base level and D2H copy of the
+generated levels inside the timed region).
+
+--impl reference times the reference's CPU implementation of this path on
+the host cores (its restatement in oracle/, since the reference itself cannot
+be built on every host) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+HEADLINE = (16384, 16384)
+CONFIGS = [(4096, 4096), (4095, 4095), (4094, 4094), (1920, 1080), (2048, 2048)]
+L2_FLUSH_BYTES = 512 << 20
+
+
+def algorithmic_bytes(w: int, h: int, bpp: int = 4, first: int = 0, last: int | None = None) -> int:
+    """One read of level `first` plus one write of levels first+1..last."""
+    from vk_compute_mipmaps_gb300.pyramid import level_sizes
+    sizes = level_sizes(w, h)
+    last = len(sizes) - 1 if last is None else last
+    lw, lh = sizes[first]
+    return bpp * (lw * lh + sum(a * b for a, b in sizes[first + 1:last + 1]))
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_key: str):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return d.get(kernel_key)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        import torch
+        try:
+            u = str(torch.cuda.get_device_properties(device).uuid)
+            self.gpu = u if u.startswith("GPU-") else f"GPU-{u}"
+        except Exception:
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+            self.gpu = vis.split(",")[device.index or 0] if vis else str(device.index or 0)
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.file:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, smax, reasons = [], [], set()
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+
+def make_chain(w, h, dev, seed=1234):
+    import torch
+    import vk_compute_mipmaps_gb300 as V
+    chain = V.MipChain(w, h, V.PRESET_SRGBA8, device=dev)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    chain.storage[:chain.offsets[1]].copy_(
+        torch.randint(0, 256, (chain.offsets[1],), generator=g, device=dev, dtype=torch.uint8))
+    return chain
+
+
+class Runner:
+    """Records one chain's dispatches once per call and launches them on `stream`."""
+
+    def __init__(self, chain, stream, mip_levels=0, flags=0):
+        import vk_compute_mipmaps_gb300 as V
+        self.V = V
+        self.chain, self.stream, self.mips, self.flags = chain, stream, mip_levels, flags
+        self.pipes = V.Pipelines(V.PRESET_SRGBA8)
+        self.cmd = V.Cmd(flags)
+        self.image = chain.image()
+
+        self.lib = V._native.load()
+        self.args = (self.cmd.handle, stream.cuda_stream, self.pipes.struct, ctypes.byref(self.image), mip_levels)
+
+    def __call__(self):
+        rc = self.lib.nvproPyramidGenerate(*self.args)
+        if rc:
+            self.V._native.check(rc, "nvproPyramidGenerate")
+        return self.lib.nvproPyramidCmdLaunchCount(self.args[0])
+
+
+def time_loop(fn, stream, steps, warmup, flush=None):
+    """Per-step device times (ms) with CUDA events on `stream`."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        fn()
+        e.record(stream)
+        times.append((s, e))
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in times]
+
+
+def bench_config(w, h, dev, stream, flush, steps):
+    chain = make_chain(w, h, dev)
+    run = Runner(chain, stream)
+    with __import__("torch").cuda.stream(stream):
+        cold = time_loop(run, stream, steps, 3, flush=flush)
+        warm = time_loop(run, stream, steps, 3)
+    nbytes = algorithmic_bytes(w, h)
+    peak, _ = measured_peak()
+    out = {}
+    for name, ts in (("l2_flushed", cold), ("warm", warm)):
+        us = statistics.median(ts) * 1e3
+        out[name] = {"us_per_chain": round(us, 2), "us_min": round(min(ts) * 1e3, 2),
+                     "GBps": round(nbytes / (us * 1e-6) / 1e9, 1),
+                     "frac_of_hbm_peak": round(nbytes / (us * 1e-6) / 1e9 / peak, 4)}
+    out["launches_per_chain"] = run()
+    out["algorithmic_bytes"] = nbytes
+    del chain
+    return out
+
+
+def cpu_baseline_sample(threads: int, reps: int = 1):
+    """The restated reference CPU generator on `threads` host threads, one
+    4096^2 image per thread (as the reference benchmark runs one image per
+    thread, demo_app/mipmaps_app.cpp:642-654).  Returns us per 16384^2-chain
+    equivalent (16 x 4096^2 = the 16384^2 base in texels)."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT / "tests"))
+    import _oracle as O
+    w = h = 4096
+    bases = [np.random.default_rng(i).integers(0, 256, (h, w, 4), dtype=np.uint8) for i in range(threads)]
+    bufs = [O.packed_from_base(1, b) for b in bases]
+    lib = O.orc()
+
+    def work(buf):
+        for _ in range(reps):
+            lib.orc_refcpu_srgba8(w, h, buf.ctypes.data_as(O.POINTER(O.c_uint8)))
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(b,)) for b in bufs]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    dt = time.perf_counter() - t0
+    chains_4096 = threads * reps
+    scale = algorithmic_bytes(*HEADLINE) / algorithmic_bytes(w, h)
+    us_per_16384 = dt / chains_4096 * scale * 1e6
+    return us_per_16384, dt, f"{chains_4096} x 4096^2 chains on {threads} threads ({dt:.2f} s), scaled by bytes"
+
+
+def run_ours(args, rank, world):
+    import torch
+    import vk_compute_mipmaps_gb300 as V
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(dev)
+    peak, peak_kind = measured_peak()
+    w, h = HEADLINE
+
+    chain = make_chain(w, h, dev)
+    run = Runner(chain, stream)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            run()
+        torch.cuda.synchronize()
+        barrier(world)
+        launches = 0
+        with ClockSampler(dev) as clk:
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            for _ in range(args.steps):
+                launches += run()
+            e.record(stream)
+            torch.cuda.synchronize()
+        ms = s.elapsed_time(e)
+    ms = max_over_ranks(ms, world)
+    ms_per_step = ms / args.steps
+    us_per_chain = ms_per_step * 1e3 / world  # whole job: world chains per step
+    chain_bytes = algorithmic_bytes(w, h)
+
+    # Dominant kernel: the first launch of the chain.  If the chain is one
+    # launch (tail fused), that launch is the chain; otherwise time the first
+    # dispatch alone (mipLevels = 7: the F6 over level 0).
+    launches_per_chain = run()
+    if launches_per_chain == 1:
+        kruns, kbytes, kname = run, chain_bytes, "fast_tma_f6_fused_tail"
+    else:
+        kruns = Runner(chain, stream, mip_levels=7)
+        kbytes, kname = algorithmic_bytes(w, h, last=6), "fast_f6_level0"
+    with torch.cuda.stream(stream):
+        kt = time_loop(kruns, stream, max(20, min(args.steps, 200)), 3)
+    k_ms = statistics.mean(kt)
+    achieved = kbytes / (k_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(kname)
+
+    extra = {"chain_GBps": round(chain_bytes / (ms_per_step * 1e-3) / 1e9, 1),
+             "chain_frac_of_hbm_peak": round(chain_bytes / (ms_per_step * 1e-3) / 1e9 / peak, 4),
+             "chain_algorithmic_bytes": chain_bytes, "launches_per_chain": launches_per_chain}
+    e2e = None
+    cpu = None
+    if rank == 0:
+        # End to end through the public API with host buffers.
+        base_host = torch.empty(chain.offsets[1], dtype=torch.uint8, pin_memory=True)
+        base_host.copy_(chain.storage[:chain.offsets[1]])
+        out_host = torch.empty(chain.offsets[-1] - chain.offsets[1], dtype=torch.uint8, pin_memory=True)
+
+        def e2e_step():
+            chain.storage[:chain.offsets[1]].copy_(base_host, non_blocking=True)
+            run()
+            out_host.copy_(chain.storage[chain.offsets[1]:], non_blocking=True)
+
+        n_e2e = max(3, min(args.steps, 20))
+        with torch.cuda.stream(stream):
+            et = time_loop(e2e_step, stream, n_e2e, 2)
+        e2e_us = statistics.mean(et) * 1e3
+        e2e = {"value": round(e2e_us, 2), "unit": "us", "h2d_bytes_per_step": base_host.numel(),
+               "d2h_bytes_per_step": out_host.numel(), "steps": n_e2e}
+        del base_host, out_host
+        if not args.no_extra:
+            flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+            del chain
+            torch.cuda.empty_cache()
+            for cw, ch in CONFIGS:
+                extra[f"{cw}x{ch}"] = bench_config(cw, ch, dev, stream, flush, max(10, min(args.steps, 100)))
+            del flush
+        if not args.no_cpu:
+            threads = os.cpu_count() or 1
+            us, dt, sample = cpu_baseline_sample(threads)
+            cpu = {"value": round(us, 1), "unit": "us per 16384^2 chain", "cores": threads, "kind": "port",
+                   "sample": sample}
+
+    line = {
+        "metric": "srgba8_16384x16384_full_chain_us",
+        "value": round(us_per_chain, 2),
+        "unit": "us",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 5),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u8",
+        "data": "synthetic: uniform random bytes (torch.Generator seed 1234)",
+        "config": {"workload": "sRGBA8 16384x16384 full 15-level chain, reference schedule F6 F6 F2",
+                   "image": "16384x16384", "preset": "srgba8", "levels": 15,
+                   "l2": "inputs larger than L2 (1 GiB base level)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "algorithmic_bytes_per_launch": kbytes, "launch_us": round(k_ms * 1e3, 2),
+                     "peak_kind": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "extra": extra,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU generator (restated in oracle/) on all host cores."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline_sample(threads)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        us, dt, sample = cpu_baseline_sample(threads)
+        vals.append(us)
+    total = time.perf_counter() - t0
+    v = statistics.mean(vals)
+    line = {
+        "impl": "reference",
+        "metric": "srgba8_16384x16384_full_chain_us",
+        "value": round(v, 1),
+        "unit": "us",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total / args.steps * 1e3, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u8",
+        "data": "synthetic: uniform random bytes",
+        "config": {"workload": "sRGBA8 16384x16384 full 15-level chain", "image": "16384x16384",
+                   "preset": "srgba8", "levels": 15},
+        "cpu_baseline": {"value": round(v, 1), "unit": "us", "cores": threads, "kind": "port",
+                         "sample": sample + "; cpuGenerateMipmaps_sRGBA restated (oracle/pyr_oracle.cpp), "
+                                            "bit-exact to the reference build"},
+        "e2e": {"value": round(v, 1), "unit": "us", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other image sizes")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args(argv)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_ours(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,262 @@
+/*
+ * nvpro_pyramid_cuda.h -- C ABI of the GB300 image-pyramid (mipmap) engine.
+ *
+ * This is the drop-in replacement for the host side of nvpro_pyramid
+ * (nvpro_pyramid/nvpro_pyramid_dispatch.hpp in nvpro-samples/vk_compute_mipmaps).
+ * The reference records Vulkan compute dispatches onto a VkCommandBuffer; this
+ * library records the same dispatch sequence into an NvproPyramidCmd and, at
+ * nvproPyramidEndCmd, launches CUDA kernels for sm_103a onto a CUDA stream.
+ *
+ * Mapping of reference concepts:
+ *   VkCommandBuffer            -> NvproPyramidCmd (recorder bound to a cudaStream_t)
+ *   VkPipeline (fast/general)  -> NvproPyramidPipeline (preset + fast/general kernels)
+ *   descriptor sets            -> NvproPyramidImage (per-level device pointers)
+ *   push constant (4 bytes)    -> nvproPyramidCmdPushConstants, same encoding
+ *                                 (inputLevel << 5 | levelCount)
+ *   vkCmdDispatch              -> nvproPyramidCmdDispatch (same workgroup counts)
+ *   vkCmdPipelineBarrier       -> nvproPyramidCmdPipelineBarrier (stream order)
+ *   assert() in the dispatcher -> NvproPyramidResult error codes
+ *
+ * All functions are plain C: no C++ or torch types cross this boundary.
+ * Device memory is owned by the caller; the library allocates device memory
+ * only in nvproPyramidCreateCmd (a few bytes of counters), never while
+ * recording or launching.
+ */
+#ifndef NVPRO_PYRAMID_CUDA_H_
+#define NVPRO_PYRAMID_CUDA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define NVPRO_PYRAMID_API __declspec(dllexport)
+#else
+#define NVPRO_PYRAMID_API __attribute__((visibility("default")))
+#endif
+
+/* A CUDA stream (cudaStream_t / CUstream); NULL is the legacy default stream. */
+typedef struct CUstream_st* NvproPyramidStream;
+
+/* Replaces the reference's assert()s (nvpro_pyramid_dispatch.hpp:169,172). */
+typedef enum NvproPyramidResult {
+  NVPRO_PYRAMID_SUCCESS                = 0,
+  NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT = 1, /* null pointer, bad size, level out of range */
+  NVPRO_PYRAMID_ERROR_INVALID_STATE    = 2, /* e.g. dispatch with no bound pipeline or image */
+  NVPRO_PYRAMID_ERROR_DISPATCHER       = 3, /* dispatcher returned 0 or more than remainingLevels */
+  NVPRO_PYRAMID_ERROR_UNSUPPORTED      = 4, /* preset / layout not supported by a kernel */
+  NVPRO_PYRAMID_ERROR_CUDA             = 5, /* a CUDA runtime call failed */
+  NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY    = 6,
+  NVPRO_PYRAMID_ERROR_TIMEOUT          = 7  /* a bounded device-side wait gave up */
+} NvproPyramidResult;
+
+/* Static description of a result code. */
+NVPRO_PYRAMID_API const char* nvproPyramidResultString(NvproPyramidResult result);
+/* Human-readable detail of the last error raised on the calling thread ("" if none). */
+NVPRO_PYRAMID_API const char* nvproPyramidLastError(void);
+
+/* ------------------------------------------------------------------------ */
+/* Pipelines.  The reference compiles one fast and one general VkPipeline    */
+/* per preset (srgba8_mipmap_{fast,general}_pipeline.comp); here a pipeline  */
+/* names a preset and which of the two kernel families it runs.              */
+/* ------------------------------------------------------------------------ */
+
+typedef enum NvproPyramidPreset {
+  /* nvpro_pyramid/srgba8_mipmap_preamble.glsl:10-128: RGBA8 texels, RGB
+   * sRGB-encoded, alpha linear; reductions in linear FP32; 4 bytes/texel. */
+  NVPRO_PYRAMID_PRESET_SRGBA8  = 1,
+  /* Linear RGBA FP32 texels (16 bytes/texel).  No reference preset; the
+   * template admits any NVPRO_PYRAMID_TYPE (nvpro_pyramid.glsl:44-46). */
+  NVPRO_PYRAMID_PRESET_RGBA32F = 2,
+  /* Linear RGBA FP16 storage (8 bytes/texel), FP32 arithmetic. */
+  NVPRO_PYRAMID_PRESET_RGBA16F = 3
+} NvproPyramidPreset;
+
+typedef struct NvproPyramidPipeline_T* NvproPyramidPipeline;
+
+/* Create the fast (isFastPipeline != 0; nvpro_pyramid.glsl:209-534) or the
+ * general (nvpro_pyramid.glsl:536-885) pipeline of a preset.  Replaces the
+ * vkCreateComputePipelines calls of minimal_app/minimal_mipmaps.cpp:178-190. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCreatePipeline(
+    NvproPyramidPreset preset, uint32_t isFastPipeline, NvproPyramidPipeline* pPipeline);
+NVPRO_PYRAMID_API void nvproPyramidDestroyPipeline(NvproPyramidPipeline pipeline);
+
+/* Bytes per texel of a preset (0 for an unknown preset). */
+NVPRO_PYRAMID_API uint32_t nvproPyramidPresetTexelBytes(NvproPyramidPreset preset);
+
+/* NvproPyramidPipelines (nvpro_pyramid_dispatch.hpp:29-35).  `layout` is an
+ * opaque caller pointer handed unchanged to the dispatcher callbacks (the
+ * VkPipelineLayout slot); pushConstantOffset must be 0 (the 4-byte push
+ * constant has no other home here). */
+typedef struct NvproPyramidPipelines {
+  NvproPyramidPipeline generalPipeline; /* mandatory */
+  NvproPyramidPipeline fastPipeline;    /* optional (NULL) */
+  const void*          layout;
+  uint32_t             pushConstantOffset;
+} NvproPyramidPipelines;
+
+/* ------------------------------------------------------------------------ */
+/* Images (the descriptor sets of srgba8_mipmap_preamble.glsl:10-13).        */
+/* ------------------------------------------------------------------------ */
+
+#define NVPRO_PYRAMID_MAX_LEVELS 32
+
+/* Level k has size max(width >> k, 1) x max(height >> k, 1)
+ * (nvpro_pyramid_dispatch.hpp:175-178; include/mipmap_storage.hpp:67-69).
+ * levels[k] is the device address of texel (0,0) of level k; rows are
+ * rowPitchBytes[k] apart (0 = tightly packed). */
+typedef struct NvproPyramidImage {
+  uint32_t width;
+  uint32_t height;
+  uint32_t levelCount; /* number of valid entries of levels[] */
+  uint32_t reserved;
+  void*    levels[NVPRO_PYRAMID_MAX_LEVELS];
+  uint64_t rowPitchBytes[NVPRO_PYRAMID_MAX_LEVELS];
+} NvproPyramidImage;
+
+/* Number of levels of a full chain: floor(log2(max(w, h))) + 1
+ * (nvpro_pyramid_dispatch.hpp:122-132).  0 if w == h == 0. */
+NVPRO_PYRAMID_API uint32_t nvproPyramidFullLevelCount(uint32_t width, uint32_t height);
+
+/* Byte offset of each level in the packed layout of MipmapStorage
+ * (include/mipmap_storage.hpp:53-76): levels contiguous, each [y][x].
+ * Writes levelCount + 1 offsets (the last one is the total size). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidPackedLayout(
+    uint32_t width, uint32_t height, uint32_t levelCount, uint32_t bytesPerTexel,
+    uint64_t* pOffsets);
+
+/* Fill an NvproPyramidImage for a packed allocation starting at `base`. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidImageInitPacked(
+    NvproPyramidImage* pImage, void* base, uint32_t width, uint32_t height,
+    uint32_t levelCount, uint32_t bytesPerTexel);
+
+/* ------------------------------------------------------------------------ */
+/* Command recording (VkCommandBuffer analogue).                             */
+/* ------------------------------------------------------------------------ */
+
+typedef struct NvproPyramidCmd_T* NvproPyramidCmd;
+
+/* Record, but launch nothing at nvproPyramidEndCmd (no CUDA call at all). */
+#define NVPRO_PYRAMID_CMD_RECORD_ONLY 0x1u
+/* Launch one kernel per recorded dispatch (no in-kernel tail fusion). */
+#define NVPRO_PYRAMID_CMD_NO_FUSION 0x2u
+/* Use only the portable (plain load/store) kernels, never the TMA kernels. */
+#define NVPRO_PYRAMID_CMD_PORTABLE_KERNELS 0x4u
+
+/* A command object is externally synchronised, like a VkCommandBuffer: one
+ * thread records it, and its launches must not overlap another submission of
+ * the same object on the GPU (they share its device counters). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCreateCmd(uint32_t flags, NvproPyramidCmd* pCmd);
+NVPRO_PYRAMID_API void nvproPyramidDestroyCmd(NvproPyramidCmd cmd);
+
+/* vkBeginCommandBuffer: clears previous records and binds the stream. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBeginCmd(NvproPyramidCmd cmd, NvproPyramidStream stream);
+/* vkEndCommandBuffer + vkQueueSubmit: lowers the recorded dispatches to
+ * kernel launches on the stream.  Returns the first error raised while
+ * recording, if any (then nothing is launched). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd);
+
+/* vkCmdBindDescriptorSets: the image every later dispatch reads and writes. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdBindImage(NvproPyramidCmd cmd, const NvproPyramidImage* pImage);
+/* vkCmdBindPipeline (nvpro_pyramid_dispatch.hpp:213,262). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdBindPipeline(NvproPyramidCmd cmd, NvproPyramidPipeline pipeline);
+/* vkCmdPushConstants (nvpro_pyramid_dispatch.hpp:231,269): 4 bytes at offset 0. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdPushConstants(
+    NvproPyramidCmd cmd, const void* layout, uint32_t offset, uint32_t size, const void* pValues);
+/* vkCmdDispatch (nvpro_pyramid_dispatch.hpp:238,282,289).  Workgroup counts
+ * have the reference's meaning (fast: 256-thread groups over 1024 or 4096
+ * input samples; general: 128 outputs or one 8x8 tile of the second level);
+ * a smaller count leaves the reference's uncovered texels unwritten. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdDispatch(
+    NvproPyramidCmd cmd, uint32_t groupCountX, uint32_t groupCountY, uint32_t groupCountZ);
+/* vkCmdPipelineBarrier (nvpro_pyramid_dispatch.hpp:183-186). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdPipelineBarrier(NvproPyramidCmd cmd);
+
+/* One recorded dispatch, for inspection and tests. */
+typedef struct NvproPyramidDispatchRecord {
+  uint32_t isFastPipeline;
+  uint32_t preset;
+  uint32_t pushConstant; /* inputLevel << 5 | levelCount */
+  uint32_t groupCountX;
+  uint32_t groupCountY;
+  uint32_t groupCountZ;
+  uint32_t pipelineBound;  /* a bind preceded this dispatch */
+  uint32_t barrierBefore;  /* a barrier preceded this dispatch */
+} NvproPyramidDispatchRecord;
+
+NVPRO_PYRAMID_API uint32_t nvproPyramidCmdRecordCount(NvproPyramidCmd cmd);
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdGetRecords(
+    NvproPyramidCmd cmd, NvproPyramidDispatchRecord* pRecords, uint32_t count);
+/* Kernel launches issued by the last nvproPyramidEndCmd. */
+NVPRO_PYRAMID_API uint32_t nvproPyramidCmdLaunchCount(NvproPyramidCmd cmd);
+
+/* ------------------------------------------------------------------------ */
+/* The dispatcher (nvpro_pyramid_dispatch.hpp:54-304).                       */
+/* ------------------------------------------------------------------------ */
+
+#define NVPRO_PYRAMID_INPUT_LEVEL_SHIFT 5u /* nvproPyramidInputLevelShift, :77 */
+
+/* NvproPyramidState (nvpro_pyramid_dispatch.hpp:63-75). */
+typedef struct NvproPyramidState {
+  uint32_t currentLevel;
+  uint32_t remainingLevels;
+  uint32_t currentX;
+  uint32_t currentY;
+} NvproPyramidState;
+
+/* nvpro_pyramid_dispatcher_t (nvpro_pyramid_dispatch.hpp:99-104): record one
+ * bind (if pipelineIfNeeded != NULL), push constant and dispatch; return the
+ * number of levels filled.  A fast dispatcher may return 0 to decline; a
+ * general dispatcher must not. */
+typedef uint32_t (*nvpro_pyramid_dispatcher_t)(
+    NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
+    NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state);
+
+/* nvproCmdPyramidDispatch with the default dispatchers
+ * (nvpro_pyramid_dispatch.hpp:54-59, :294-304).  mipLevels == 0 means the
+ * full chain.  Requires a bound image with at least mipLevels levels. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproCmdPyramidDispatch(
+    NvproPyramidCmd cmdBuf, NvproPyramidPipelines pipelines, uint32_t baseWidth,
+    uint32_t baseHeight, uint32_t mipLevels);
+
+/* The base overload with caller dispatchers (nvpro_pyramid_dispatch.hpp:109-188). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproCmdPyramidDispatchEx(
+    NvproPyramidCmd cmdBuf, NvproPyramidPipelines pipelines, uint32_t baseWidth,
+    uint32_t baseHeight, uint32_t mipLevels, nvpro_pyramid_dispatcher_t generalDispatcher,
+    nvpro_pyramid_dispatcher_t fastDispatcher);
+
+/* nvproPyramidDefaultFastDispatcher<4, 6> (nvpro_pyramid_dispatch.hpp:195-242). */
+NVPRO_PYRAMID_API uint32_t nvproPyramidDefaultFastDispatcher(
+    NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
+    NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state);
+
+/* The body of nvproPyramidDefaultFastDispatcher<DivisibilityRequirement,
+ * MaxLevels> for any even DivisibilityRequirement and MaxLevels in 1..6, for
+ * C callers that cannot instantiate the template (e.g. the <2, 5> and <2, 6>
+ * variants registered in demo_app/nvpro_pyramid_dispatch_alternative.cpp:41-42). */
+NVPRO_PYRAMID_API uint32_t nvproPyramidFastDispatch(
+    NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
+    NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state,
+    uint32_t divisibilityRequirement, uint32_t maxLevels);
+
+/* nvproPyramidDefaultGeneralDispatcher (nvpro_pyramid_dispatch.hpp:247-292). */
+NVPRO_PYRAMID_API uint32_t nvproPyramidDefaultGeneralDispatcher(
+    NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
+    NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state);
+
+/* Begin + bind image + nvproCmdPyramidDispatch + End in one call: the whole
+ * sequence of minimal_app/minimal_mipmaps.cpp:199-210 (bind descriptor sets,
+ * dispatch, submit) for callers that record nothing else.  The image's
+ * width/height are the base size. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerate(
+    NvproPyramidCmd cmd, NvproPyramidStream stream, NvproPyramidPipelines pipelines,
+    const NvproPyramidImage* pImage, uint32_t mipLevels);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* NVPRO_PYRAMID_CUDA_H_ */

@@ -1,0 +1,167 @@
+"""The C ABI without a GPU: the library loads, exports every symbol the header
+declares, records exactly the reference dispatcher's command sequence, and
+turns the reference's asserts into error codes.  Commands here are created
+with NVPRO_PYRAMID_CMD_RECORD_ONLY, which makes no CUDA call."""
+import ctypes
+import gzip
+import json
+import re
+from pathlib import Path
+
+import pytest
+
+import _oracle as O
+from vk_compute_mipmaps_gb300 import _native as N
+from vk_compute_mipmaps_gb300 import pyramid as P
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def header_functions():
+    names = set()
+    for hdr in (ROOT / "include").glob("*.h"):
+        src = hdr.read_text()
+        names |= set(re.findall(r"NVPRO_PYRAMID_API\s+[\w\s\*]+?\b(\w+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_function(native):
+    names = header_functions()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(native, name), name
+    assert names <= set(N.SIGNATURES), names - set(N.SIGNATURES)
+
+
+def fake_image(w, h, levels=0, bpp=4):
+    """An image whose level pointers are aligned but never dereferenced."""
+    levels = levels or P.full_level_count(w, h)
+    return P.make_image([0x7F0000000000 + 0x100000 * k for k in range(levels)], w, h)
+
+
+def record(w, h, mips=0, has_fast=True, general=None, fast=None, preset=N.PRESET_SRGBA8):
+    cmd = P.Cmd(N.CMD_RECORD_ONLY)
+    pipes = P.Pipelines(preset, fast=has_fast)
+    cmd.begin(None)
+    cmd.bind_image(fake_image(w, h))
+    P.cmd_pyramid_dispatch(cmd, pipes, w, h, mips, general=general, fast=fast)
+    cmd.end()
+    return cmd.records()
+
+
+def records_to_events(recs):
+    ev = []
+    for r in recs:
+        if r["barrierBefore"]:
+            ev.append([4, 0, 0, 0])
+        if r["pipelineBound"]:
+            ev.append([1, r["isFastPipeline"], 0, 0])
+        ev.append([2, r["pushConstant"], 0, 4])
+        ev.append([3, r["groupCountX"], r["groupCountY"], r["groupCountZ"]])
+    return ev
+
+
+def test_records_match_reference_dispatcher_golden(native):
+    with gzip.open(ROOT / "tests" / "golden" / "dispatch_schedules.json.gz", "rt") as f:
+        golden = json.load(f)
+
+    def fast_variant(div, mx):
+        return P.wrap_dispatcher(lambda c, lay, pco, pipe, st: native.nvproPyramidFastDispatch(
+            c, lay, pco, pipe, ctypes.byref(st), div, mx))
+
+    null = P.wrap_dispatcher(lambda c, lay, pco, pipe, st: st.remainingLevels)
+    fasts = {1: fast_variant(2, 5), 2: fast_variant(2, 6), 3: null}
+    checked = 0
+    for key, events in golden.items():
+        w, h, mips, has_fast, var = map(int, key.split(","))
+        if checked > 2500 and w < 2047 and (w + h) % 3:
+            continue  # keep the CPU suite quick: a large deterministic subset
+        general = null if var == 4 else None
+        fast = fasts.get(var)
+        recs = record(w, h, mips, bool(has_fast), general=general, fast=fast)
+        # A barrier after the last dispatch (possible when a null dispatcher
+        # records nothing) orders nothing; records keep barriers as a flag of
+        # the following dispatch, so such a barrier has no record.
+        while events and events[-1][0] == 4:
+            events = events[:-1]
+        assert records_to_events(recs) == events, key
+        checked += 1
+    assert checked > 2500
+
+
+def expect_error(code, fn):
+    with pytest.raises(N.NativeLibraryError) as e:
+        fn()
+    assert e.value.code == code, str(e.value)
+
+
+def test_error_codes_replace_asserts(native):
+    pipes = P.Pipelines()
+    cmd = P.Cmd(N.CMD_RECORD_ONLY)
+    # more levels than the image size allows
+    cmd.begin(None)
+    cmd.bind_image(fake_image(16, 16))
+    expect_error(N.ERROR_INVALID_ARGUMENT, lambda: P.cmd_pyramid_dispatch(cmd, pipes, 16, 16, 6))
+    # general dispatcher returning 0 (the reference asserts levelsDone != 0)
+    cmd.begin(None)
+    cmd.bind_image(fake_image(15, 15))
+    zero = P.wrap_dispatcher(lambda *a: 0)
+    expect_error(N.ERROR_DISPATCHER, lambda: P.cmd_pyramid_dispatch(cmd, pipes, 15, 15, general=zero))
+    # ... and more than remainingLevels (levelsDone <= state.remainingLevels)
+    cmd.begin(None)
+    cmd.bind_image(fake_image(15, 15))
+    many = P.wrap_dispatcher(lambda c, l, o, p, st: st.remainingLevels + 1)
+    expect_error(N.ERROR_DISPATCHER, lambda: P.cmd_pyramid_dispatch(cmd, pipes, 15, 15, general=many))
+    expect_error(N.ERROR_DISPATCHER, cmd.end)  # the error is sticky until End
+    # dispatch without a bound image
+    cmd.begin(None)
+    expect_error(N.ERROR_INVALID_STATE, lambda: P.cmd_pyramid_dispatch(cmd, pipes, 8, 8))
+    # the image has fewer levels than the dispatch writes
+    cmd.begin(None)
+    cmd.bind_image(fake_image(64, 64, levels=3))
+    expect_error(N.ERROR_INVALID_ARGUMENT, lambda: P.cmd_pyramid_dispatch(cmd, pipes, 64, 64))
+    # push constant must be 4 bytes at offset 0
+    cmd.begin(None)
+    v = ctypes.c_uint32(1)
+    expect_error(N.ERROR_INVALID_ARGUMENT,
+                 lambda: N.check(native.nvproPyramidCmdPushConstants(cmd.handle, None, 4, 4, ctypes.byref(v))))
+    # misaligned level pointer
+    cmd.begin(None)
+    img = fake_image(8, 8)
+    img.levels[1] = img.levels[1] + 2
+    cmd.bind_image(img)
+    expect_error(N.ERROR_UNSUPPORTED, lambda: P.cmd_pyramid_dispatch(cmd, pipes, 8, 8))
+    # unknown preset, missing general pipeline
+    h = ctypes.c_void_p()
+    expect_error(N.ERROR_UNSUPPORTED, lambda: N.check(native.nvproPyramidCreatePipeline(9, 0, ctypes.byref(h))))
+    cmd.begin(None)
+    cmd.bind_image(fake_image(8, 8))
+    bad = N.NvproPyramidPipelines(None, pipes.fast, None, 0)
+    expect_error(N.ERROR_INVALID_ARGUMENT,
+                 lambda: N.check(native.nvproCmdPyramidDispatch(cmd.handle, bad, 8, 8, 0)))
+    expect_error(N.ERROR_INVALID_ARGUMENT, cmd.end)  # reports the recorded error
+    # End without Begin
+    expect_error(N.ERROR_INVALID_STATE, cmd.end)
+    # null handles are rejected, not dereferenced
+    expect_error(N.ERROR_INVALID_ARGUMENT, lambda: N.check(native.nvproPyramidBeginCmd(None, None)))
+
+
+def test_single_level_image_records_nothing(native):
+    assert record(1, 1) == []
+
+
+def test_packed_layout_matches_mipmap_storage(native):
+    for w, h in [(1, 1), (3, 5), (64, 64), (4095, 17), (16384, 16384)]:
+        levels = P.full_level_count(w, h)
+        offs = (ctypes.c_uint64 * (levels + 1))()
+        N.check(native.nvproPyramidPackedLayout(w, h, levels, 4, offs))
+        assert list(offs) == O.offsets(w, h, levels, 4) == P.packed_offsets(w, h, levels, 4)
+        assert native.nvproPyramidFullLevelCount(w, h) == O.full_levels(w, h) == levels
+
+
+def test_partial_mip_count_and_general_only(native):
+    recs = record(64, 64, mips=3)
+    assert [(r["isFastPipeline"], r["pushConstant"] & 31) for r in recs] == [(1, 2)]
+    recs = record(64, 64, has_fast=False)
+    assert all(r["isFastPipeline"] == 0 for r in recs)
+    assert sum(r["pushConstant"] & 31 for r in recs) == 6

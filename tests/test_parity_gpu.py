@@ -1,0 +1,239 @@
+"""GPU parity: the CUDA kernels, called through the C ABI, against the CPU
+oracle on the same seeded inputs -- bit-exact for every preset.
+
+Outputs are pre-filled with a sentinel (the reference pre-clears to magenta,
+demo_app/mipmaps_app.cpp:688-705) so unwritten texels show up.  Sizes cover
+every schedule branch (docs/test_images.txt: 1080p, 4094, 4095, 2052, 4096 ...)
+plus 1xN, Nx1, 2^k +- 1 and tiny images.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import _oracle as O
+from vk_compute_mipmaps_gb300 import _native as N
+from vk_compute_mipmaps_gb300 import pyramid as P
+
+pytestmark = pytest.mark.gpu
+
+SENTINEL = 0xA7
+
+SIZES = [(1, 1), (2, 1), (1, 2), (1, 9), (9, 1), (2, 2), (3, 3), (4, 4), (5, 5), (7, 3), (8, 8), (12, 20),
+         (16, 16), (17, 17), (31, 31), (32, 32), (33, 33), (63, 64), (64, 64), (65, 65), (65, 33), (96, 160),
+         (127, 129), (128, 128), (255, 256), (256, 256), (257, 257), (1024, 1), (1, 1024), (1000, 3),
+         (513, 512), (640, 384), (1920, 1080), (2052, 2052), (2047, 2047)]
+BIG = [(4096, 4096), (4095, 4095), (4094, 4094), (2048, 2048), (3840, 2160), (2560, 1440)]
+FLAGS = [0, N.CMD_NO_FUSION, N.CMD_PORTABLE_KERNELS]
+
+
+def random_base(preset, w, h, seed):
+    rng = np.random.default_rng(seed)
+    if preset == N.PRESET_SRGBA8:
+        return rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    if preset == N.PRESET_RGBA32F:
+        return rng.lognormal(0.0, 1.0, (h, w, 4)).astype(np.float32)
+    return rng.lognormal(0.0, 1.0, (h, w, 4)).astype(np.float16)
+
+
+def oracle_bytes(preset, base, schedule, mips):
+    h, w = base.shape[:2]
+    off = O.offsets(w, h, mips, O.BPP[preset])
+    buf = np.full(off[-1], SENTINEL, np.uint8)
+    buf[:off[1]] = np.ascontiguousarray(base).view(np.uint8).reshape(-1)
+    return O.run(preset, w, h, buf, schedule, mips)
+
+
+def gpu_run(cuda, preset, base, flags=0, mips=0, general=None, fast=None, has_fast=True):
+    """Generate on the GPU; return (packed bytes, recorded schedule, launches)."""
+    import torch
+    h, w = base.shape[:2]
+    mips = mips or P.full_level_count(w, h)
+    chain = P.MipChain(w, h, preset, mips, device=cuda)
+    chain.storage.fill_(SENTINEL)
+    raw = torch.from_numpy(np.ascontiguousarray(base).view(np.uint8).reshape(-1).copy())
+    chain.storage[:chain.offsets[1]].copy_(raw)
+    cmd = P.Cmd(flags)
+    pipes = P.Pipelines(preset, fast=has_fast)
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    cmd.begin(stream)
+    cmd.bind_image(chain.image())
+    P.cmd_pyramid_dispatch(cmd, pipes, w, h, mips, general=general, fast=fast)
+    cmd.end()
+    torch.cuda.synchronize()
+    sched = [(r["isFastPipeline"], r["pushConstant"],
+              r["groupCountX"] if r["groupCountY"] and r["groupCountZ"] else 0) for r in cmd.records()]
+    return chain.storage.cpu().numpy(), sched, cmd.launch_count
+
+
+def assert_same(got, want, w, h, bpp, mips, what):
+    if np.array_equal(got, want):
+        return
+    off = O.offsets(w, h, mips, bpp)
+    for k in range(mips):
+        a, b = got[off[k]:off[k + 1]], want[off[k]:off[k + 1]]
+        if not np.array_equal(a, b):
+            idx = np.nonzero(a != b)[0]
+            lw = max(w >> k, 1)
+            t = idx[0] // bpp
+            raise AssertionError(f"{what}: level {k} differs at {len(idx)} bytes; first texel "
+                                 f"({t % lw}, {t // lw}) got {a[t*bpp:(t+1)*bpp]} want {b[t*bpp:(t+1)*bpp]}")
+
+
+@pytest.mark.parametrize("flags", FLAGS)
+@pytest.mark.parametrize("w,h", SIZES)
+def test_srgba8_bit_exact(cuda, w, h, flags):
+    base = random_base(N.PRESET_SRGBA8, w, h, w * 131 + h)
+    got, sched, _ = gpu_run(cuda, N.PRESET_SRGBA8, base, flags)
+    mips = P.full_level_count(w, h)
+    assert sched == [tuple(s) for s in O.default_schedule(w, h)]
+    assert_same(got, oracle_bytes(N.PRESET_SRGBA8, base, sched, mips), w, h, 4, mips, f"{w}x{h} flags={flags}")
+
+
+@pytest.mark.parametrize("w,h", BIG)
+def test_srgba8_bit_exact_large(cuda, w, h):
+    from test_oracle_pins import smooth_field
+    base = smooth_field(w, h, 5, opaque=False)
+    mips = P.full_level_count(w, h)
+    want = None
+    for flags in FLAGS:
+        got, sched, _ = gpu_run(cuda, N.PRESET_SRGBA8, base, flags)
+        if want is None:
+            want = oracle_bytes(N.PRESET_SRGBA8, base, sched, mips)
+        assert_same(got, want, w, h, 4, mips, f"{w}x{h} flags={flags}")
+
+
+@pytest.mark.parametrize("preset", [N.PRESET_RGBA32F, N.PRESET_RGBA16F])
+@pytest.mark.parametrize("w,h", [(1, 1), (3, 3), (64, 64), (65, 33), (256, 256), (257, 129), (1920, 1080),
+                                 (1023, 777)])
+def test_float_presets_bit_exact(cuda, preset, w, h):
+    base = random_base(preset, w, h, 99 + w)
+    mips = P.full_level_count(w, h)
+    for flags in (0, N.CMD_PORTABLE_KERNELS):
+        got, sched, _ = gpu_run(cuda, preset, base, flags)
+        assert_same(got, oracle_bytes(preset, base, sched, mips), w, h, O.BPP[preset], mips, f"{preset} {w}x{h}")
+
+
+def fast_variant(div, mx):
+    lib = N.load()
+    return P.wrap_dispatcher(lambda c, lay, pco, pipe, st: lib.nvproPyramidFastDispatch(
+        c, lay, pco, pipe, ctypes.byref(st), div, mx))
+
+
+def partial_general(fraction):
+    """The default general dispatcher, but dispatching only part of the grid."""
+    lib = N.load()
+
+    def fn(c, lay, pco, pipe, st):
+        if pipe:
+            lib.nvproPyramidCmdBindPipeline(c, pipe)
+        levels = min(2, st.remainingLevels)
+        pc = ctypes.c_uint32(st.currentLevel << 5 | levels)
+        lib.nvproPyramidCmdPushConstants(c, lay, pco, 4, ctypes.byref(pc))
+        dw, dh = max(st.currentX >> levels, 1), max(st.currentY >> levels, 1)
+        full = -(-dw * dh // 128) if levels == 1 else -(-dw // 8) * -(-dh // 8)
+        lib.nvproPyramidCmdDispatch(c, int(full * fraction), 1, 1)
+        return levels
+    return P.wrap_dispatcher(fn)
+
+
+def partial_fast(fraction):
+    lib = N.load()
+
+    def fn(c, lay, pco, pipe, st):
+        if st.currentX % 4 or st.currentY % 4:
+            return 0
+        if pipe:
+            lib.nvproPyramidCmdBindPipeline(c, pipe)
+        x, y, n = st.currentX, st.currentY, 0
+        while x % 2 == 0 and y % 2 == 0 and n < st.remainingLevels and n < 6:
+            x, y, n = x // 2, y // 2, n + 1
+        pc = ctypes.c_uint32(st.currentLevel << 5 | n)
+        lib.nvproPyramidCmdPushConstants(c, lay, pco, 4, ctypes.byref(pc))
+        per = 4096 if n > 5 else 1024
+        lib.nvproPyramidCmdDispatch(c, int(-(-st.currentX * st.currentY // per) * fraction), 1, 1)
+        return n
+    return P.wrap_dispatcher(fn)
+
+
+null = None
+
+
+@pytest.mark.parametrize("case", ["levels_1_5", "levels_1_6", "general_only", "null_fast",
+                                  "partial_general", "partial_fast", "null_general"])
+@pytest.mark.parametrize("w,h", [(64, 64), (96, 40), (1920, 1080), (255, 257), (2052, 2052), (640, 384)])
+def test_custom_dispatchers(cuda, case, w, h):
+    """Dispatcher variants of demo_app/nvpro_pyramid_dispatch_alternative.cpp:41-77,
+    and dispatchers that cover only part of the grid: the GPU writes exactly
+    what the oracle writes for the recorded schedule (sentinel elsewhere)."""
+    nul = P.wrap_dispatcher(lambda c, lay, pco, pipe, st: st.remainingLevels)
+    kw = {"levels_1_5": dict(fast=fast_variant(2, 5)), "levels_1_6": dict(fast=fast_variant(2, 6)),
+          "general_only": dict(has_fast=False), "null_fast": dict(fast=nul),
+          "partial_general": dict(general=partial_general(0.6)), "partial_fast": dict(fast=partial_fast(0.3)),
+          "null_general": dict(general=nul)}[case]
+    base = random_base(N.PRESET_SRGBA8, w, h, 7 * w + h)
+    mips = P.full_level_count(w, h)
+    for flags in FLAGS:
+        got, sched, _ = gpu_run(cuda, N.PRESET_SRGBA8, base, flags, **kw)
+        assert_same(got, oracle_bytes(N.PRESET_SRGBA8, base, sched, mips), w, h, 4, mips, f"{case} {flags}")
+
+
+@pytest.mark.parametrize("w,h", [(64, 64), (257, 129), (1920, 1080)])
+def test_pitched_separate_levels(cuda, w, h):
+    """Levels in separate allocations with padded row pitches."""
+    import torch
+    base = random_base(N.PRESET_SRGBA8, w, h, 3 * w + h)
+    mips = P.full_level_count(w, h)
+    sizes = P.level_sizes(w, h, mips)
+    pitches = [((lw * 4 + 255) // 256) * 256 + 64 for lw, _ in sizes]
+    bufs = [torch.full((lh * p,), SENTINEL, dtype=torch.uint8, device=cuda) for (lw, lh), p in zip(sizes, pitches)]
+    bufs[0].view(h, pitches[0])[:, :w * 4].copy_(torch.from_numpy(base.reshape(h, w * 4)))
+    img = P.make_image([b.data_ptr() for b in bufs], w, h, pitches)
+    for flags in FLAGS:
+        cmd, pipes = P.Cmd(flags), P.Pipelines()
+        cmd.begin(torch.cuda.current_stream(cuda).cuda_stream)
+        cmd.bind_image(img)
+        P.cmd_pyramid_dispatch(cmd, pipes, w, h)
+        cmd.end()
+        torch.cuda.synchronize()
+        want = O.pyramid(1, base)
+        off = O.offsets(w, h, mips, 4)
+        for k, ((lw, lh), p) in enumerate(zip(sizes, pitches)):
+            got = bufs[k].view(lh, p)[:, :lw * 4].cpu().numpy().reshape(-1)
+            assert np.array_equal(got, want[off[k]:off[k + 1]]), (flags, k)
+
+
+def test_16384_chain_tile_local_and_tail(cuda):
+    """The 16384^2 benchmark chain (F6, F6, F2) at full size, through
+    size-independent properties: every 64x64 tile of level 0 determines its
+    levels 1..6 alone (checked on random tiles against the oracle), the top
+    levels 7..14 follow from level 6 alone (checked against the oracle run on
+    the GPU's level 6), and all kernel paths write identical bytes."""
+    import torch
+    w = h = 16384
+    g = torch.Generator(device=cuda).manual_seed(1234)
+    chain = P.MipChain(w, h, N.PRESET_SRGBA8, device=cuda)
+    chain.storage.fill_(SENTINEL)
+    chain.storage[:chain.offsets[1]].copy_(
+        torch.randint(0, 256, (chain.offsets[1],), generator=g, device=cuda, dtype=torch.uint8))
+    results = []
+    for flags in FLAGS:
+        chain.storage[chain.offsets[1]:].fill_(SENTINEL)
+        P.generate(chain, flags=flags)
+        torch.cuda.synchronize()
+        results.append(chain.storage[chain.offsets[1]:].clone())
+    for r in results[1:]:
+        assert torch.equal(results[0], r)
+    rng = np.random.default_rng(5)
+    for _ in range(12):
+        tx, ty = rng.integers(0, 256, 2)
+        tile = chain.level(0)[ty * 64:(ty + 1) * 64, tx * 64:(tx + 1) * 64].cpu().numpy()
+        want = O.split_levels(O.pyramid(1, tile, schedule=[(1, 6, 1)], mips=7), 64, 64, 7, 4, np.uint8)
+        for k in range(1, 7):
+            e = 64 >> k
+            got = chain.level(k)[ty * e:(ty + 1) * e, tx * e:(tx + 1) * e].cpu().numpy()
+            assert np.array_equal(got, want[k]), (tx, ty, k)
+    lvl6 = chain.level(6).cpu().numpy()
+    want = O.split_levels(O.pyramid(1, lvl6), 256, 256, 9, 4, np.uint8)
+    for k in range(1, 9):
+        assert np.array_equal(chain.level(6 + k).cpu().numpy(), want[k]), k

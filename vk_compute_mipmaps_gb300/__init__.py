@@ -1,0 +1,19 @@
+"""GB300-native image-pyramid (mipmap) engine with the operator surface of
+nvpro_pyramid (nvpro-samples/vk_compute_mipmaps).
+
+The product is the native library libnvpro_pyramid_cuda.so (C ABI in
+include/nvpro_pyramid_cuda.h, CUDA kernels for sm_103a).  This package loads
+it through ctypes and adds torch conveniences; it has no CPU fallback.
+"""
+from . import _native
+from ._native import (CMD_NO_FUSION, CMD_PORTABLE_KERNELS, CMD_RECORD_ONLY, PRESET_RGBA16F, PRESET_RGBA32F,
+                      PRESET_SRGBA8, NativeLibraryError, NvproPyramidImage, NvproPyramidState)
+from .pyramid import (Cmd, MipChain, Pipelines, cmd_pyramid_dispatch, full_level_count, generate, level_sizes,
+                      make_image, packed_offsets, wrap_dispatcher)
+
+__all__ = [
+    "CMD_NO_FUSION", "CMD_PORTABLE_KERNELS", "CMD_RECORD_ONLY", "PRESET_RGBA16F", "PRESET_RGBA32F",
+    "PRESET_SRGBA8", "NativeLibraryError", "NvproPyramidImage", "NvproPyramidState", "Cmd", "MipChain",
+    "Pipelines", "cmd_pyramid_dispatch", "full_level_count", "generate", "level_sizes", "make_image",
+    "packed_offsets", "wrap_dispatcher",
+]

@@ -1,0 +1,540 @@
+// api.cpp -- the C ABI of include/nvpro_pyramid_cuda.h: pipelines, images,
+// the command recorder and the level scheduler (nvproCmdPyramidDispatch).
+//
+// Recording mirrors nvpro_pyramid_dispatch.hpp call for call.  At
+// nvproPyramidEndCmd the recorded dispatches are lowered to kernel launches
+// on the command's stream; stream order takes the place of the reference's
+// compute->compute barriers.  Small trailing dispatches may be folded into
+// the tail of the preceding kernel (NVPRO_PYRAMID_CMD_NO_FUSION disables it);
+// the bytes written are the same either way.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/nvpro_pyramid_cuda.h"
+#include "internal.h"
+
+using namespace nvpyr;
+
+namespace {
+
+thread_local std::string t_lastError;
+
+NvproPyramidResult fail(NvproPyramidResult r, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_lastError = buf;
+  return r;
+}
+
+constexpr uint32_t kPipelineMagic = 0x50595250u;  // "PRYP"
+constexpr uint32_t kCmdMagic = 0x434D4450u;       // "PDMC"
+
+uint32_t levelDim(uint32_t base, uint32_t k) {
+  const uint32_t d = k >= 32 ? 0u : base >> k;
+  return d ? d : 1u;
+}
+
+}  // namespace
+
+struct NvproPyramidPipeline_T {
+  uint32_t magic;
+  uint32_t preset;
+  uint32_t isFast;
+};
+
+struct Record {
+  NvproPyramidDispatchRecord info;
+  NvproPyramidImage image;
+};
+
+struct NvproPyramidCmd_T {
+  uint32_t magic;
+  uint32_t flags;
+  cudaStream_t stream = nullptr;
+  bool recording = false;
+  bool imageBound = false;
+  NvproPyramidImage image{};
+  NvproPyramidPipeline pipeline = nullptr;
+  bool pipelineBoundSinceDispatch = false;
+  bool barrierSinceDispatch = false;
+  uint32_t pushConstant = 0;
+  bool pushConstantSet = false;
+  NvproPyramidResult error = NVPRO_PYRAMID_SUCCESS;
+  std::string errorText;
+  std::vector<Record> records;
+  uint32_t launches = 0;
+  Scratch scratch{nullptr, 0};
+};
+
+namespace {
+
+bool validCmd(NvproPyramidCmd cmd) { return cmd && cmd->magic == kCmdMagic; }
+bool validPipeline(NvproPyramidPipeline p) { return p && p->magic == kPipelineMagic; }
+
+// Record a sticky error on the command (reported again by nvproPyramidEndCmd).
+NvproPyramidResult cmdFail(NvproPyramidCmd cmd, NvproPyramidResult r, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_lastError = buf;
+  if (validCmd(cmd) && cmd->error == NVPRO_PYRAMID_SUCCESS) {
+    cmd->error = r;
+    cmd->errorText = buf;
+  }
+  return r;
+}
+
+// Build kernel parameters for a record; checks the image against the dispatch.
+NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
+  const NvproPyramidImage& img = rec.image;
+  const uint32_t L = rec.info.pushConstant >> NVPRO_PYRAMID_INPUT_LEVEL_SHIFT;
+  const uint32_t n = rec.info.pushConstant & 31u;
+  const uint32_t bpp = presetBytes(rec.info.preset);
+  if (n == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "dispatch with level count 0");
+  if (rec.info.isFastPipeline ? n > kMaxDispatchLevels : n > 2)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%s pipeline cannot fill %u levels in one dispatch",
+                rec.info.isFastPipeline ? "fast" : "general", n);
+  if (uint64_t(L) + n >= img.levelCount)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "dispatch writes level %u but the image has %u levels",
+                L + n, img.levelCount);
+  std::memset(out, 0, sizeof *out);
+  out->preset = rec.info.preset;
+  out->isFast = rec.info.isFastPipeline;
+  out->inputLevel = L;
+  out->levelCount = n;
+  out->groups = (rec.info.groupCountY == 0 || rec.info.groupCountZ == 0) ? 0 : rec.info.groupCountX;
+  const uint32_t align = bpp == 4 ? 4 : bpp == 8 ? 8 : 16;
+  for (uint32_t k = 0; k <= n; ++k) {
+    const uint32_t lvl = L + k;
+    LevelView& v = out->lv[k];
+    v.w = levelDim(img.width, lvl);
+    v.h = levelDim(img.height, lvl);
+    v.ptr = static_cast<uint8_t*>(img.levels[lvl]);
+    v.pitch = img.rowPitchBytes[lvl] ? img.rowPitchBytes[lvl] : uint64_t(v.w) * bpp;
+    if (!v.ptr) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "level %u has no device pointer", lvl);
+    if (v.pitch < uint64_t(v.w) * bpp)
+      return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "level %u row pitch %llu < %u texels", lvl,
+                  (unsigned long long)v.pitch, v.w);
+    if ((reinterpret_cast<uintptr_t>(v.ptr) % align) || (v.pitch % align))
+      return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "level %u pointer/pitch not %u-byte aligned", lvl, align);
+  }
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+// Index of the last record that the TMA kernel may absorb as its in-kernel
+// tail: fast dispatches whose input level is small enough that one CTA
+// finishes it quickly (the reference pays a whole dispatch plus a barrier).
+constexpr uint64_t kTailMaxTexels = 64u * 64u;
+
+}  // namespace
+
+extern "C" {
+
+const char* nvproPyramidResultString(NvproPyramidResult r) {
+  switch (r) {
+    case NVPRO_PYRAMID_SUCCESS: return "success";
+    case NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case NVPRO_PYRAMID_ERROR_INVALID_STATE: return "invalid state";
+    case NVPRO_PYRAMID_ERROR_DISPATCHER: return "dispatcher contract violated";
+    case NVPRO_PYRAMID_ERROR_UNSUPPORTED: return "unsupported";
+    case NVPRO_PYRAMID_ERROR_CUDA: return "CUDA error";
+    case NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY: return "out of memory";
+    case NVPRO_PYRAMID_ERROR_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown result";
+}
+
+const char* nvproPyramidLastError(void) { return t_lastError.c_str(); }
+
+uint32_t nvproPyramidPresetTexelBytes(NvproPyramidPreset preset) { return presetBytes(uint32_t(preset)); }
+
+NvproPyramidResult nvproPyramidCreatePipeline(NvproPyramidPreset preset, uint32_t isFastPipeline,
+                                              NvproPyramidPipeline* pPipeline) {
+  if (!pPipeline) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pPipeline is NULL");
+  *pPipeline = nullptr;
+  if (presetBytes(uint32_t(preset)) == 0)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "unknown preset %d", int(preset));
+  auto* p = new (std::nothrow) NvproPyramidPipeline_T{kPipelineMagic, uint32_t(preset), isFastPipeline ? 1u : 0u};
+  if (!p) return fail(NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY, "host allocation failed");
+  *pPipeline = p;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+void nvproPyramidDestroyPipeline(NvproPyramidPipeline pipeline) {
+  if (validPipeline(pipeline)) {
+    pipeline->magic = 0;
+    delete pipeline;
+  }
+}
+
+uint32_t nvproPyramidFullLevelCount(uint32_t width, uint32_t height) {
+  uint32_t m = 0;
+  while (width != 0 || height != 0) {
+    width >>= 1;
+    height >>= 1;
+    ++m;
+  }
+  return m;
+}
+
+NvproPyramidResult nvproPyramidPackedLayout(uint32_t width, uint32_t height, uint32_t levelCount,
+                                            uint32_t bytesPerTexel, uint64_t* pOffsets) {
+  if (!pOffsets) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pOffsets is NULL");
+  if (width == 0 || height == 0 || bytesPerTexel == 0)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "zero width, height or texel size");
+  if (levelCount == 0 || levelCount > nvproPyramidFullLevelCount(width, height))
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "level count %u outside 1..%u", levelCount,
+                nvproPyramidFullLevelCount(width, height));
+  uint64_t off = 0;
+  for (uint32_t k = 0; k < levelCount; ++k) {
+    pOffsets[k] = off;
+    off += uint64_t(levelDim(width, k)) * levelDim(height, k) * bytesPerTexel;
+  }
+  pOffsets[levelCount] = off;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidImageInitPacked(NvproPyramidImage* pImage, void* base, uint32_t width,
+                                               uint32_t height, uint32_t levelCount, uint32_t bytesPerTexel) {
+  if (!pImage || !base) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "NULL image or base pointer");
+  if (levelCount > NVPRO_PYRAMID_MAX_LEVELS)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "level count %u > %u", levelCount,
+                NVPRO_PYRAMID_MAX_LEVELS);
+  uint64_t off[NVPRO_PYRAMID_MAX_LEVELS + 1];
+  NvproPyramidResult r = nvproPyramidPackedLayout(width, height, levelCount, bytesPerTexel, off);
+  if (r != NVPRO_PYRAMID_SUCCESS) return r;
+  std::memset(pImage, 0, sizeof *pImage);
+  pImage->width = width;
+  pImage->height = height;
+  pImage->levelCount = levelCount;
+  for (uint32_t k = 0; k < levelCount; ++k) {
+    pImage->levels[k] = static_cast<uint8_t*>(base) + off[k];
+    pImage->rowPitchBytes[k] = uint64_t(levelDim(width, k)) * bytesPerTexel;
+  }
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidCreateCmd(uint32_t flags, NvproPyramidCmd* pCmd) {
+  if (!pCmd) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pCmd is NULL");
+  *pCmd = nullptr;
+  auto* c = new (std::nothrow) NvproPyramidCmd_T();
+  if (!c) return fail(NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY, "host allocation failed");
+  c->magic = kCmdMagic;
+  c->flags = flags;
+  if (!(flags & NVPRO_PYRAMID_CMD_RECORD_ONLY)) {
+    // Counters for in-kernel tail fusion: allocated once here, never while
+    // recording or launching.
+    const uint32_t count = 1024;
+    void* ptr = nullptr;
+    cudaError_t e = cudaMalloc(&ptr, count * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ptr, 0, count * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+      if (ptr) cudaFree(ptr);
+      delete c;
+      return fail(e == cudaErrorMemoryAllocation ? NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY : NVPRO_PYRAMID_ERROR_CUDA,
+                  "cudaMalloc of command counters failed: %s", cudaGetErrorString(e));
+    }
+    c->scratch.counters = static_cast<uint32_t*>(ptr);
+    c->scratch.counterCount = count;
+  }
+  *pCmd = c;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+void nvproPyramidDestroyCmd(NvproPyramidCmd cmd) {
+  if (!validCmd(cmd)) return;
+  if (cmd->scratch.counters) cudaFree(cmd->scratch.counters);
+  cmd->magic = 0;
+  delete cmd;
+}
+
+NvproPyramidResult nvproPyramidBeginCmd(NvproPyramidCmd cmd, NvproPyramidStream stream) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  cmd->stream = reinterpret_cast<cudaStream_t>(stream);
+  cmd->recording = true;
+  cmd->imageBound = false;
+  cmd->pipeline = nullptr;
+  cmd->pipelineBoundSinceDispatch = false;
+  cmd->barrierSinceDispatch = false;
+  cmd->pushConstantSet = false;
+  cmd->error = NVPRO_PYRAMID_SUCCESS;
+  cmd->errorText.clear();
+  cmd->records.clear();
+  cmd->launches = 0;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidCmdBindImage(NvproPyramidCmd cmd, const NvproPyramidImage* pImage) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->recording) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  if (!pImage) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pImage is NULL");
+  if (pImage->width == 0 || pImage->height == 0)
+    return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "image has zero width or height");
+  if (pImage->levelCount == 0 || pImage->levelCount > NVPRO_PYRAMID_MAX_LEVELS ||
+      pImage->levelCount > nvproPyramidFullLevelCount(pImage->width, pImage->height))
+    return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "image level count %u invalid for %ux%u",
+                   pImage->levelCount, pImage->width, pImage->height);
+  cmd->image = *pImage;
+  cmd->imageBound = true;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidCmdBindPipeline(NvproPyramidCmd cmd, NvproPyramidPipeline pipeline) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->recording) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  if (!validPipeline(pipeline)) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid pipeline");
+  cmd->pipeline = pipeline;
+  cmd->pipelineBoundSinceDispatch = true;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidCmdPushConstants(NvproPyramidCmd cmd, const void* /*layout*/, uint32_t offset,
+                                                uint32_t size, const void* pValues) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->recording) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  if (!pValues || offset != 0 || size != 4)
+    return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT,
+                   "push constant must be 4 bytes at offset 0 (got %u at %u)", size, offset);
+  std::memcpy(&cmd->pushConstant, pValues, 4);
+  cmd->pushConstantSet = true;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidCmdDispatch(NvproPyramidCmd cmd, uint32_t gx, uint32_t gy, uint32_t gz) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->recording) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  if (!cmd->pipeline) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "dispatch with no bound pipeline");
+  if (!cmd->imageBound) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "dispatch with no bound image");
+  if (!cmd->pushConstantSet)
+    return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "dispatch with no push constant set");
+  Record r;
+  std::memset(&r, 0, sizeof r);
+  r.info.isFastPipeline = cmd->pipeline->isFast;
+  r.info.preset = cmd->pipeline->preset;
+  r.info.pushConstant = cmd->pushConstant;
+  r.info.groupCountX = gx;
+  r.info.groupCountY = gy;
+  r.info.groupCountZ = gz;
+  r.info.pipelineBound = cmd->pipelineBoundSinceDispatch;
+  r.info.barrierBefore = cmd->barrierSinceDispatch;
+  r.image = cmd->image;
+  DispatchParams probe;
+  NvproPyramidResult res = makeParams(r, &probe);
+  if (res != NVPRO_PYRAMID_SUCCESS) return cmdFail(cmd, res, "%s", t_lastError.c_str());
+  cmd->records.push_back(r);
+  cmd->pipelineBoundSinceDispatch = false;
+  cmd->barrierSinceDispatch = false;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidCmdPipelineBarrier(NvproPyramidCmd cmd) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->recording) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  cmd->barrierSinceDispatch = true;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+uint32_t nvproPyramidCmdRecordCount(NvproPyramidCmd cmd) {
+  return validCmd(cmd) ? uint32_t(cmd->records.size()) : 0u;
+}
+
+NvproPyramidResult nvproPyramidCmdGetRecords(NvproPyramidCmd cmd, NvproPyramidDispatchRecord* pRecords,
+                                             uint32_t count) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (count > cmd->records.size() || (count && !pRecords))
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "asked for %u of %zu records", count, cmd->records.size());
+  for (uint32_t i = 0; i < count; ++i) pRecords[i] = cmd->records[i].info;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+uint32_t nvproPyramidCmdLaunchCount(NvproPyramidCmd cmd) { return validCmd(cmd) ? cmd->launches : 0u; }
+
+NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->recording) return fail(NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  cmd->recording = false;
+  cmd->launches = 0;
+  if (cmd->error != NVPRO_PYRAMID_SUCCESS) {
+    t_lastError = cmd->errorText;
+    return cmd->error;
+  }
+  if (cmd->flags & NVPRO_PYRAMID_CMD_RECORD_ONLY) return NVPRO_PYRAMID_SUCCESS;
+
+  std::vector<DispatchParams> params(cmd->records.size());
+  for (size_t i = 0; i < cmd->records.size(); ++i) {
+    NvproPyramidResult r = makeParams(cmd->records[i], &params[i]);
+    if (r != NVPRO_PYRAMID_SUCCESS) return r;
+  }
+  const bool fuse = !(cmd->flags & NVPRO_PYRAMID_CMD_NO_FUSION);
+  const bool portableOnly = (cmd->flags & NVPRO_PYRAMID_CMD_PORTABLE_KERNELS) != 0;
+  size_t i = 0;
+  while (i < params.size()) {
+    const DispatchParams& p = params[i];
+    cudaError_t e;
+    if (!portableOnly && p.isFast && tmaFastSupported(p)) {
+      // Absorb following small dispatches of the same image into this
+      // kernel's tail (last-CTA-done), if every one of them is small.
+      size_t tail = 0;
+      if (fuse) {
+        size_t j = i + 1;
+        while (j < params.size() && params[j].preset == p.preset &&
+               uint64_t(params[j].lv[0].w) * params[j].lv[0].h <= kTailMaxTexels &&
+               cmd->records[j].image.levels[0] == cmd->records[i].image.levels[0])
+          ++j;
+        tail = j - i - 1;
+      }
+      e = launchTmaFast(p, tail ? &params[i + 1] : nullptr, uint32_t(tail), cmd->stream, cmd->scratch,
+                        &cmd->launches);
+      i += 1 + tail;
+    } else {
+      e = launchPortable(p, cmd->stream, &cmd->launches);
+      i += 1;
+    }
+    if (e != cudaSuccess)
+      return fail(NVPRO_PYRAMID_ERROR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  }
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// The dispatcher (nvpro_pyramid_dispatch.hpp:109-304).
+
+uint32_t nvproPyramidFastDispatch(NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
+                                  NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state,
+                                  uint32_t divisibilityRequirement, uint32_t maxLevels) {
+  if (!state || divisibilityRequirement == 0 || divisibilityRequirement % 2 != 0 || maxLevels == 0 ||
+      maxLevels > 6) {
+    cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT,
+            "fast dispatcher needs an even divisibility requirement and 1..6 levels");
+    return 0;
+  }
+  if (state->currentX % divisibilityRequirement != 0 || state->currentY % divisibilityRequirement != 0) return 0;
+  if (pipelineIfNeeded) nvproPyramidCmdBindPipeline(cmdBuf, pipelineIfNeeded);
+  uint32_t x = state->currentX, y = state->currentY, levels = 0;
+  while (x % 2 == 0 && y % 2 == 0 && levels < state->remainingLevels && levels < maxLevels) {
+    x /= 2;
+    y /= 2;
+    ++levels;
+  }
+  const uint32_t pc = state->currentLevel << NVPRO_PYRAMID_INPUT_LEVEL_SHIFT | levels;
+  nvproPyramidCmdPushConstants(cmdBuf, layout, pushConstantOffset, sizeof pc, &pc);
+  // 4096 input samples per workgroup for 6 levels, else 1024 (:234-238);
+  // the product wraps in 32 bits exactly as the reference computes it.
+  const uint32_t shift = levels > 5 ? 12u : 10u, mask = levels > 5 ? 4095u : 1023u;
+  const uint32_t samples = state->currentX * state->currentY;
+  nvproPyramidCmdDispatch(cmdBuf, (samples + mask) >> shift, 1u, 1u);
+  return levels;
+}
+
+uint32_t nvproPyramidDefaultFastDispatcher(NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
+                                           NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state) {
+  return nvproPyramidFastDispatch(cmdBuf, layout, pushConstantOffset, pipelineIfNeeded, state, 4, 6);
+}
+
+uint32_t nvproPyramidDefaultGeneralDispatcher(NvproPyramidCmd cmdBuf, const void* layout,
+                                              uint32_t pushConstantOffset, NvproPyramidPipeline pipelineIfNeeded,
+                                              const NvproPyramidState* state) {
+  // "py2_4_8_8" parameters (:254-258): 4 warps, 8x8 tiles, at most 2 levels.
+  constexpr uint32_t kMaxLevels = 2, kThreads = 4 * 32, kTile = 8;
+  if (!state) {
+    cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "state is NULL");
+    return 0;
+  }
+  if (pipelineIfNeeded) nvproPyramidCmdBindPipeline(cmdBuf, pipelineIfNeeded);
+  const uint32_t levels = state->remainingLevels >= kMaxLevels ? kMaxLevels : state->remainingLevels;
+  const uint32_t pc = state->currentLevel << NVPRO_PYRAMID_INPUT_LEVEL_SHIFT | levels;
+  nvproPyramidCmdPushConstants(cmdBuf, layout, pushConstantOffset, sizeof pc, &pc);
+  uint32_t dstW = state->currentX >> levels, dstH = state->currentY >> levels;
+  dstW = dstW ? dstW : 1u;
+  dstH = dstH ? dstH : 1u;
+  if (levels == 1)
+    nvproPyramidCmdDispatch(cmdBuf, (dstW * dstH + (kThreads - 1)) / kThreads, 1u, 1u);
+  else
+    nvproPyramidCmdDispatch(cmdBuf, ((dstW + kTile - 1) / kTile) * ((dstH + kTile - 1) / kTile), 1u, 1u);
+  return levels;
+}
+
+NvproPyramidResult nvproCmdPyramidDispatchEx(NvproPyramidCmd cmdBuf, NvproPyramidPipelines pipelines,
+                                             uint32_t baseWidth, uint32_t baseHeight, uint32_t mipLevels,
+                                             nvpro_pyramid_dispatcher_t generalDispatcher,
+                                             nvpro_pyramid_dispatcher_t fastDispatcher) {
+  if (!validCmd(cmdBuf)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmdBuf->recording) return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  if (!validPipeline(pipelines.generalPipeline))
+    return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "generalPipeline is mandatory");
+  if (pipelines.fastPipeline && !validPipeline(pipelines.fastPipeline))
+    return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid fastPipeline");
+  if (pipelines.pushConstantOffset != 0)
+    return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_UNSUPPORTED, "pushConstantOffset must be 0");
+  if (!generalDispatcher || (pipelines.fastPipeline && !fastDispatcher))
+    return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "missing dispatcher callback");
+  if (baseWidth == 0 || baseHeight == 0)
+    return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "zero base width or height");
+  const uint32_t fullLevels = nvproPyramidFullLevelCount(baseWidth, baseHeight);
+  if (mipLevels == 0) mipLevels = fullLevels;  // :122-132
+  if (mipLevels > fullLevels)
+    return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u levels requested; %ux%u has at most %u",
+                   mipLevels, baseWidth, baseHeight, fullLevels);
+  // A single-level image needs no dispatch (the reference asserts here,
+  // because its loop dispatches before testing remainingLevels).
+  if (mipLevels == 1) return NVPRO_PYRAMID_SUCCESS;
+
+  NvproPyramidState state{0u, mipLevels - 1u, baseWidth, baseHeight};
+  NvproPyramidPipeline fastIfNeeded = pipelines.fastPipeline;
+  NvproPyramidPipeline generalIfNeeded = pipelines.generalPipeline;
+  while (true) {
+    uint32_t done = 0;
+    if (pipelines.fastPipeline)
+      done = fastDispatcher(cmdBuf, pipelines.layout, pipelines.pushConstantOffset, fastIfNeeded, &state);
+    if (done != 0) {
+      fastIfNeeded = nullptr;
+      generalIfNeeded = pipelines.generalPipeline;
+    } else {
+      done = generalDispatcher(cmdBuf, pipelines.layout, pipelines.pushConstantOffset, generalIfNeeded, &state);
+      fastIfNeeded = pipelines.fastPipeline;
+      generalIfNeeded = nullptr;
+    }
+    if (cmdBuf->error != NVPRO_PYRAMID_SUCCESS) return cmdBuf->error;
+    if (done == 0 || done > state.remainingLevels)  // the reference's asserts (:169,:172)
+      return cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_DISPATCHER,
+                     "dispatcher filled %u levels with %u remaining at level %u", done, state.remainingLevels,
+                     state.currentLevel);
+    state.currentLevel += done;
+    state.remainingLevels -= done;
+    state.currentX = std::max(state.currentX >> done, 1u);
+    state.currentY = std::max(state.currentY >> done, 1u);
+    if (state.remainingLevels == 0) break;
+    nvproPyramidCmdPipelineBarrier(cmdBuf);
+  }
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproCmdPyramidDispatch(NvproPyramidCmd cmdBuf, NvproPyramidPipelines pipelines,
+                                           uint32_t baseWidth, uint32_t baseHeight, uint32_t mipLevels) {
+  return nvproCmdPyramidDispatchEx(cmdBuf, pipelines, baseWidth, baseHeight, mipLevels,
+                                   nvproPyramidDefaultGeneralDispatcher, nvproPyramidDefaultFastDispatcher);
+}
+
+NvproPyramidResult nvproPyramidGenerate(NvproPyramidCmd cmd, NvproPyramidStream stream,
+                                        NvproPyramidPipelines pipelines, const NvproPyramidImage* pImage,
+                                        uint32_t mipLevels) {
+  NvproPyramidResult r = nvproPyramidBeginCmd(cmd, stream);
+  if (r != NVPRO_PYRAMID_SUCCESS) return r;
+  nvproPyramidCmdBindImage(cmd, pImage);
+  if (pImage) nvproCmdPyramidDispatch(cmd, pipelines, pImage->width, pImage->height, mipLevels);
+  return nvproPyramidEndCmd(cmd);
+}
+
+}  // extern "C"

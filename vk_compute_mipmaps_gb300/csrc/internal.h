@@ -1,0 +1,49 @@
+// internal.h -- host-side types shared between the C ABI (api.cpp) and the
+// kernel translation units.  Not part of the public interface.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nvpyr {
+
+constexpr uint32_t kMaxDispatchLevels = 6;  // fast pipeline: 1..6 levels (nvpro_pyramid.glsl:221-225)
+
+enum Preset : uint32_t { kSrgba8 = 1, kRgba32f = 2, kRgba16f = 3 };
+
+inline uint32_t presetBytes(uint32_t preset) {
+  return preset == kSrgba8 ? 4u : preset == kRgba32f ? 16u : preset == kRgba16f ? 8u : 0u;
+}
+
+// One level of an image as a kernel sees it.
+struct LevelView {
+  uint8_t* ptr;
+  uint64_t pitch;  // bytes between rows
+  uint32_t w, h;
+};
+
+// Everything one recorded dispatch needs: the reference's push constant
+// decoded, the workgroup coverage, and levels L..L+n.
+struct DispatchParams {
+  uint32_t preset;
+  uint32_t isFast;
+  uint32_t inputLevel;  // L
+  uint32_t levelCount;  // n
+  uint64_t groups;      // reference workgroups covered (gx if gy, gz > 0, else 0)
+  LevelView lv[kMaxDispatchLevels + 1];
+};
+
+// Device scratch owned by a command object (allocated at creation).
+struct Scratch {
+  uint32_t* counters;     // zero-initialised, self-resetting
+  uint32_t counterCount;
+};
+
+// Kernel families.  Each returns cudaSuccess or the launch error, and adds the
+// number of kernels it launched to *launches.
+cudaError_t launchPortable(const DispatchParams& p, cudaStream_t stream, uint32_t* launches);
+// True if the TMA fast-pipeline kernel can run this dispatch (layout, alignment).
+bool tmaFastSupported(const DispatchParams& p);
+cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, uint32_t tailCount,
+                          cudaStream_t stream, const Scratch& scratch, uint32_t* launches);
+
+}  // namespace nvpyr
