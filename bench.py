@@ -235,9 +235,10 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream(dev)
     peak, peak_kind = measured_peak()
-    w, h = HEADLINE
+    w, h = map(int, args.image.lower().split("x"))
 
     chain = make_chain(w, h, dev)
+    levels = len(chain.offsets) - 1
     run = Runner(chain, stream)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -278,7 +279,7 @@ def run_ours(args, rank, world):
              "chain_algorithmic_bytes": chain_bytes, "launches_per_chain": launches_per_chain}
     e2e = None
     cpu = None
-    if rank == 0:
+    if rank == 0 and not args.no_e2e:
         # End to end through the public API with host buffers.
         base_host = torch.empty(chain.offsets[1], dtype=torch.uint8, pin_memory=True)
         base_host.copy_(chain.storage[:chain.offsets[1]])
@@ -296,6 +297,7 @@ def run_ours(args, rank, world):
         e2e = {"value": round(e2e_us, 2), "unit": "us", "h2d_bytes_per_step": base_host.numel(),
                "d2h_bytes_per_step": out_host.numel(), "steps": n_e2e}
         del base_host, out_host
+    if rank == 0:
         if not args.no_extra:
             flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
             del chain
@@ -310,7 +312,7 @@ def run_ours(args, rank, world):
                    "sample": sample}
 
     line = {
-        "metric": "srgba8_16384x16384_full_chain_us",
+        "metric": f"srgba8_{w}x{h}_full_chain_us",
         "value": round(us_per_chain, 2),
         "unit": "us",
         "n_gpus": world,
@@ -322,8 +324,8 @@ def run_ours(args, rank, world):
         "vs_baseline": None,
         "dtype": "u8",
         "data": "synthetic: uniform random bytes (torch.Generator seed 1234)",
-        "config": {"workload": "sRGBA8 16384x16384 full 15-level chain, reference schedule F6 F6 F2",
-                   "image": "16384x16384", "preset": "srgba8", "levels": 15,
+        "config": {"workload": f"sRGBA8 {w}x{h} full chain, reference dispatch schedule",
+                   "image": f"{w}x{h}", "preset": "srgba8", "levels": levels,
                    "l2": "inputs larger than L2 (1 GiB base level)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
@@ -402,6 +404,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extra", action="store_true", help="skip the other image sizes")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) measurement")
+    ap.add_argument("--image", default="16384x16384", help="headline image WxH (smaller for profiling runs)")
     args = ap.parse_args(argv)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -193,6 +193,18 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdGetRecords(
 /* Kernel launches issued by the last nvproPyramidEndCmd. */
 NVPRO_PYRAMID_API uint32_t nvproPyramidCmdLaunchCount(NvproPyramidCmd cmd);
 
+/* Wait for the command's stream, then report NVPRO_PYRAMID_ERROR_TIMEOUT if a
+ * bounded device-side wait of one of its kernels gave up since the last query
+ * (the outputs of that submission are then incomplete).  Clears the report.
+ * No reference counterpart: Vulkan reports device loss instead. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd cmd);
+
+/* Test support (no reference counterpart): encode n floats of x (device
+ * memory, values in [0, 1]) with the kernels' fast sRGB encoder into `fast`,
+ * and with the exact threshold count into `exact`. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugSrgbEncode(
+    NvproPyramidStream stream, const float* x, uint8_t* fast, uint8_t* exact, uint64_t n);
+
 /* ------------------------------------------------------------------------ */
 /* The dispatcher (nvpro_pyramid_dispatch.hpp:54-304).                       */
 /* ------------------------------------------------------------------------ */

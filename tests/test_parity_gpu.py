@@ -237,3 +237,42 @@ def test_16384_chain_tile_local_and_tail(cuda):
     want = O.split_levels(O.pyramid(1, lvl6), 256, 256, 9, 4, np.uint8)
     for k in range(1, 9):
         assert np.array_equal(chain.level(6 + k).cpu().numpy(), want[k]), k
+
+
+def test_fast_srgb_encoder_exhaustive(cuda, native):
+    """The kernels' fast encoder (lg2/ex2 candidate + one threshold compare)
+    equals the exact threshold count for every FP32 value in [0, 1.0078]
+    (the linear values an sRGBA8 pyramid can produce lie in [0, 1])."""
+    import torch
+    lo, hi = 0, int(np.float32(1.0078).view(np.uint32))
+    chunk = 1 << 28
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    for start in range(lo, hi + 1, chunk):
+        bits = torch.arange(start, min(start + chunk, hi + 1), dtype=torch.int64, device=cuda).to(torch.int32)
+        x = bits.view(torch.float32)
+        fast = torch.empty(x.numel(), dtype=torch.uint8, device=cuda)
+        exact = torch.empty_like(fast)
+        N.check(native.nvproPyramidDebugSrgbEncode(stream, x.data_ptr(), fast.data_ptr(), exact.data_ptr(),
+                                                   x.numel()))
+        torch.cuda.synchronize()
+        bad = (fast != exact).nonzero()
+        assert bad.numel() == 0, f"{bad.numel()} mismatches, first x={x[bad[0]].item()!r}"
+    # the GPU's exact count is the CPU oracle's
+    xs = np.concatenate([np.random.default_rng(1).random(1 << 16, dtype=np.float32), O.tables()[2][:255]])
+    xt = torch.from_numpy(xs).to(cuda)
+    fast = torch.empty(xs.size, dtype=torch.uint8, device=cuda)
+    exact = torch.empty_like(fast)
+    N.check(native.nvproPyramidDebugSrgbEncode(stream, xt.data_ptr(), fast.data_ptr(), exact.data_ptr(), xs.size))
+    torch.cuda.synchronize()
+    assert np.array_equal(exact.cpu().numpy(), O.srgb_encode_array(xs))
+    assert np.array_equal(fast.cpu().numpy(), O.srgb_encode_array(xs))
+
+
+def test_no_device_wait_gave_up(cuda, native):
+    import torch
+    cmd = P.Cmd()
+    chain = P.MipChain(4096, 4096, N.PRESET_SRGBA8, device=cuda)
+    chain.storage.random_(0, 256)
+    P.generate(chain, cmd=cmd)
+    N.check(native.nvproPyramidCmdDeviceStatus(cmd.handle), "device status")
+    torch.cuda.synchronize()

@@ -109,6 +109,8 @@ SIGNATURES = {
                                             c_uint32, c_uint32]),
     "nvproPyramidDefaultGeneralDispatcher": (c_uint32, [c_void_p, c_void_p, c_uint32, c_void_p,
                                                         POINTER(NvproPyramidState)]),
+    "nvproPyramidCmdDeviceStatus": (c_int, [c_void_p]),
+    "nvproPyramidDebugSrgbEncode": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
     "nvproPyramidGenerate": (c_int, [c_void_p, c_void_p, NvproPyramidPipelines, POINTER(NvproPyramidImage),
                                      c_uint32]),
 }

@@ -133,11 +133,6 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
   return NVPRO_PYRAMID_SUCCESS;
 }
 
-// Index of the last record that the TMA kernel may absorb as its in-kernel
-// tail: fast dispatches whose input level is small enough that one CTA
-// finishes it quickly (the reference pays a whole dispatch plus a barrier).
-constexpr uint64_t kTailMaxTexels = 64u * 64u;
-
 }  // namespace
 
 extern "C" {
@@ -389,10 +384,7 @@ NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
       size_t tail = 0;
       if (fuse) {
         size_t j = i + 1;
-        while (j < params.size() && params[j].preset == p.preset &&
-               uint64_t(params[j].lv[0].w) * params[j].lv[0].h <= kTailMaxTexels &&
-               cmd->records[j].image.levels[0] == cmd->records[i].image.levels[0])
-          ++j;
+        while (j < params.size() && j - i < tmaMaxFused() && tmaTailCompatible(params[j - 1], params[j])) ++j;
         tail = j - i - 1;
       }
       e = launchTmaFast(p, tail ? &params[i + 1] : nullptr, uint32_t(tail), cmd->stream, cmd->scratch,
@@ -525,6 +517,32 @@ NvproPyramidResult nvproCmdPyramidDispatch(NvproPyramidCmd cmdBuf, NvproPyramidP
                                            uint32_t baseWidth, uint32_t baseHeight, uint32_t mipLevels) {
   return nvproCmdPyramidDispatchEx(cmdBuf, pipelines, baseWidth, baseHeight, mipLevels,
                                    nvproPyramidDefaultGeneralDispatcher, nvproPyramidDefaultFastDispatcher);
+}
+
+NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd cmd) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->scratch.counters) return NVPRO_PYRAMID_SUCCESS;
+  cudaError_t e = cudaStreamSynchronize(cmd->stream);
+  uint32_t flag = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpy(&flag, cmd->scratch.counters + kCounterError, sizeof flag, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "device status: %s", cudaGetErrorString(e));
+  if (flag) {
+    // A kernel gave up waiting: clear the flag and the tail counter it may
+    // have left behind.
+    e = cudaMemset(cmd->scratch.counters, 0, cmd->scratch.counterCount * sizeof(uint32_t));
+    if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "device status: %s", cudaGetErrorString(e));
+    return fail(NVPRO_PYRAMID_ERROR_TIMEOUT, "a device-side wait gave up; outputs are incomplete");
+  }
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidDebugSrgbEncode(NvproPyramidStream stream, const float* x, uint8_t* fast,
+                                               uint8_t* exact, uint64_t n) {
+  if (!x || !fast || !exact) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "NULL buffer");
+  cudaError_t e = launchDebugEncode(x, fast, exact, n, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "debug encode: %s", cudaGetErrorString(e));
+  return NVPRO_PYRAMID_SUCCESS;
 }
 
 NvproPyramidResult nvproPyramidGenerate(NvproPyramidCmd cmd, NvproPyramidStream stream,

@@ -43,7 +43,17 @@ struct Scratch {
 cudaError_t launchPortable(const DispatchParams& p, cudaStream_t stream, uint32_t* launches);
 // True if the TMA fast-pipeline kernel can run this dispatch (layout, alignment).
 bool tmaFastSupported(const DispatchParams& p);
+// True if `next` may run inside the tail of the TMA kernel that runs `prev`.
+bool tmaTailCompatible(const DispatchParams& prev, const DispatchParams& next);
+// Maximum number of dispatches one TMA launch runs (itself plus its tail).
+uint32_t tmaMaxFused();
 cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, uint32_t tailCount,
                           cudaStream_t stream, const Scratch& scratch, uint32_t* launches);
+// Test support: the fast sRGB encoder and the exact threshold count, per float.
+cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, cudaStream_t stream);
+
+// Scratch counter slots.
+constexpr uint32_t kCounterLastCta = 0;
+constexpr uint32_t kCounterError = 1;
 
 }  // namespace nvpyr
