@@ -200,8 +200,8 @@ NVPRO_PYRAMID_API uint32_t nvproPyramidCmdLaunchCount(NvproPyramidCmd cmd);
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd cmd);
 
 /* Test support (no reference counterpart): encode n floats of x (device
- * memory, values in [0, 1]) with the kernels' fast sRGB encoder into `fast`,
- * and with the exact threshold count into `exact`. */
+ * memory) with the kernels' fast sRGB encoder into `fast` (inputs clamped to
+ * its domain [0, 1] first), and with the exact threshold count into `exact`. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugSrgbEncode(
     NvproPyramidStream stream, const float* x, uint8_t* fast, uint8_t* exact, uint64_t n);
 

@@ -156,9 +156,6 @@ def partial_fast(fraction):
     return P.wrap_dispatcher(fn)
 
 
-null = None
-
-
 @pytest.mark.parametrize("case", ["levels_1_5", "levels_1_6", "general_only", "null_fast",
                                   "partial_general", "partial_fast", "null_general"])
 @pytest.mark.parametrize("w,h", [(64, 64), (96, 40), (1920, 1080), (255, 257), (2052, 2052), (640, 384)])
@@ -241,10 +238,10 @@ def test_16384_chain_tile_local_and_tail(cuda):
 
 def test_fast_srgb_encoder_exhaustive(cuda, native):
     """The kernels' fast encoder (lg2/ex2 candidate + one threshold compare)
-    equals the exact threshold count for every FP32 value in [0, 1.0078]
-    (the linear values an sRGBA8 pyramid can produce lie in [0, 1])."""
+    equals the exact threshold count for every FP32 value in [0, 1] (the
+    linear values an sRGBA8 pyramid can produce)."""
     import torch
-    lo, hi = 0, int(np.float32(1.0078).view(np.uint32))
+    lo, hi = 0, int(np.float32(1.0).view(np.uint32))
     chunk = 1 << 28
     stream = torch.cuda.current_stream(cuda).cuda_stream
     for start in range(lo, hi + 1, chunk):
@@ -258,7 +255,8 @@ def test_fast_srgb_encoder_exhaustive(cuda, native):
         bad = (fast != exact).nonzero()
         assert bad.numel() == 0, f"{bad.numel()} mismatches, first x={x[bad[0]].item()!r}"
     # the GPU's exact count is the CPU oracle's
-    xs = np.concatenate([np.random.default_rng(1).random(1 << 16, dtype=np.float32), O.tables()[2][:255]])
+    xs = np.concatenate([np.random.default_rng(1).random(1 << 16, dtype=np.float32), O.tables()[2][:255],
+                         np.ones(1, np.float32)])
     xt = torch.from_numpy(xs).to(cuda)
     fast = torch.empty(xs.size, dtype=torch.uint8, device=cuda)
     exact = torch.empty_like(fast)

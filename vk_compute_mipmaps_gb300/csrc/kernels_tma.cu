@@ -7,23 +7,31 @@
 // (512 threads, one per SM) holds four tile groups of four warps; each group
 // owns a two-slot ring of 16 KiB region buffers filled by
 // cp.async.bulk.tensor.2d (TMA) and completed on an mbarrier.  Inside a
-// region, warp w of the group handles source rows 16w..16w+15:
-//   level L+1: lane (cx = lane & 15, half = lane >> 4) reduces two 2x2 blocks
-//              per row pair -> 8 texels, stored as 8-byte pairs;
-//   level L+2: the half-warps exchange row pairs (shfl.xor 16), 2 texels/lane;
+// region, lane (cx = lane & 15, half = lane >> 4) of warp w of the group
+// owns level-(L+1) rows 8w + 4half + i (i = 0..3), columns 2cx and 2cx+1:
+//   level L+1: two 2x2 blocks per row pair of the buffer (LOAD_REDUCE4);
+//   level L+2: from the lane's own row pairs, 2 texels per lane;
 //   level L+3: horizontal neighbours via shfl.down 1;
 //   level L+4: shfl.xor 16 + shfl.down 2;
-//   level L+5/L+6: the group's 4x4 level-L+4 block goes through shared
-//              memory and one warp (rotating per region) finishes it.
+//   level L+5/L+6: the group's 4x4 block of level L+4 goes through shared
+//              memory to the last warp to deposit its part.
 // The operand order of every REDUCE4 follows fastVerticalFirst(n, k), so the
 // bytes equal the portable kernel's and the CPU oracle's.
+//
+// No group barrier in the steady state.  The last warp to finish reading a
+// region buffer (a shared-memory atomic count) issues the TMA for the
+// group's region two steps ahead into it; the last warp to deposit its
+// level-(L+4) values finishes levels L+5/L+6.  The exchange buffers form a
+// ring of three: a warp can be at most two regions ahead of the slowest one,
+// because the load of region i+2 waits for every warp to leave region i's
+// buffer.
 //
 // sRGB codec.  Decode is a table lookup per channel from a table replicated
 // once per lane (row c holds 32 copies of decode[c] then 32 of alpha[c]), so
 // a warp's 32 random lookups hit 32 distinct banks; the address is one PRMT.
-// Encode computes a candidate code from lg2/ex2 (error well below 0.5 code)
-// and corrects it with one comparison against the exact threshold table
-// (also replicated per lane); the result equals the exact threshold count.
+// Encode computes a candidate code from lg2/ex2 and corrects it with one
+// comparison against the exact threshold table (also replicated per lane);
+// the result equals the exact threshold count for every x in [0, 1].
 //
 // Tail fusion.  When the dispatches after this one are small fast
 // dispatches of the same image (e.g. F6 F2 after the first F6 of 16384^2),
@@ -43,27 +51,33 @@ namespace {
 
 constexpr uint32_t kTile = 64;
 constexpr uint32_t kGroups = 4;
-constexpr uint32_t kGroupThreads = 128;
+constexpr uint32_t kGroupWarps = 4;
+constexpr uint32_t kGroupThreads = kGroupWarps * 32;
 constexpr uint32_t kThreads = kGroups * kGroupThreads;
 constexpr uint32_t kStages = 2;
+constexpr uint32_t kXchgRing = 3;
 constexpr uint32_t kTileBytes = kTile * kTile * 4;
 constexpr uint32_t kMaxFused = 4;
-constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier polling
+constexpr uint32_t kWaitLimit = 1u << 16;  // bounded mbarrier polling ...
+constexpr uint32_t kWaitHintNs = 20000;    // ... of at most ~20 us each
 
 // Byte offsets inside the dynamic shared memory block.
 constexpr uint32_t kLutDecodeOff = 0;                          // 256 rows x 256 B
-constexpr uint32_t kLutThrOff = kLutDecodeOff + 256 * 256;     // 256 rows x 128 B
-constexpr uint32_t kStageOff = kLutThrOff + 256 * 128;         // [group][stage] x 16 KiB
-constexpr uint32_t kXchgOff = kStageOff + kGroups * kStages * kTileBytes;  // [group][2][16] float4
-constexpr uint32_t kBarOff = kXchgOff + kGroups * 2 * 16 * 16;             // [group][stage] mbarrier
-constexpr uint32_t kFlagOff = kBarOff + kGroups * kStages * 8;
-constexpr uint32_t kSmemBytes = kFlagOff + 16;
+constexpr uint32_t kThrRows = 255;                             // candidates stay <= 254
+constexpr uint32_t kLutThrOff = kLutDecodeOff + 256 * 256;     // 255 rows x 128 B
+constexpr uint32_t kStageOff = kLutThrOff + kThrRows * 128;    // [group][stage] x 16 KiB
+constexpr uint32_t kXchgOff = kStageOff + kGroups * kStages * kTileBytes;  // [group][ring][16] float4
+constexpr uint32_t kBarOff = kXchgOff + kGroups * kXchgRing * 16 * 16;     // [group][stage] mbarrier
+constexpr uint32_t kCntOff = kBarOff + kGroups * kStages * 8;              // [group] release, exchange
+constexpr uint32_t kSmemBytes = kCntOff + kGroups * 2 * 4;
+static_assert(kStageOff % 128 == 0, "TMA destinations need 128-byte alignment");
+static_assert(kSmemBytes <= 232448, "exceeds the 227 KiB of shared memory per CTA");
+constexpr uint32_t kDebugSmemBytes = kLutThrOff + kThrRows * 128;
 
 struct FusedStage {
   uint32_t n;
   uint32_t coverW, coverH;  // covered extent of level L: multiples of 2^n
   uint32_t regionsX, regionsY;
-  uint32_t l1Pairs;  // level L+1 accepts 8-byte stores
   const uint8_t* src;
   uint64_t srcPitch;
   uint8_t* dst[kMaxDispatchLevels + 1];
@@ -89,9 +103,9 @@ __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
   for (uint32_t it = 0; it < kWaitLimit; ++it) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(kWaitHintNs)
         : "memory");
     if (done) return true;
   }
@@ -120,38 +134,52 @@ __device__ __forceinline__ float ex2Approx(float x) {
   return r;
 }
 
-// Lane constants for the replicated tables.
+// Lane constants for the replicated tables (shared-window addresses).
 struct Lut {
+  uint32_t decBase;   // the decode table
   uint32_t laneWord;  // byte0 = 4*lane, byte1 = 4*lane + 128 (alpha half of a row)
-  uint32_t thrBase;   // kLutThrOff + 4*lane - (0x4B400000 << 7)  (see encodeChannel)
+  uint32_t thrBase;   // threshold table + 4*lane - (0x4B400000 << 7)  (see encodeChannel)
 };
 
-__device__ __forceinline__ float lutLoad(uint32_t byteOff) {
+__device__ __forceinline__ Lut makeLut(uint32_t lane) {
   extern __shared__ __align__(128) uint8_t smem[];
-  return *reinterpret_cast<const float*>(smem + byteOff);
+  const uint32_t base = smemAddr(smem);
+  Lut L;
+  L.decBase = base + kLutDecodeOff;
+  L.laneWord = (4 * lane) | ((4 * lane + 128) << 8);
+  L.thrBase = base + kLutThrOff + 4 * lane - (0x4B400000u << 7);
+  return L;
+}
+
+__device__ __forceinline__ float lds(uint32_t addr) {
+  float r;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(r) : "r"(addr));
+  return r;
 }
 
 // NVPRO_PYRAMID_LOAD of one sRGBA8 texel: decode[r], decode[g], decode[b], alpha[a].
 __device__ __forceinline__ float4 decodeTexel(uint32_t w, const Lut& L) {
   // PRMT builds (code << 8) | laneByte: row = code, column = this lane's copy.
-  return make_float4(lutLoad(kLutDecodeOff + __byte_perm(w, L.laneWord, 0x6604)),
-                     lutLoad(kLutDecodeOff + __byte_perm(w, L.laneWord, 0x6614)),
-                     lutLoad(kLutDecodeOff + __byte_perm(w, L.laneWord, 0x6624)),
-                     lutLoad(kLutDecodeOff + __byte_perm(w, L.laneWord, 0x6635)));
+  return make_float4(lds(L.decBase + __byte_perm(w, L.laneWord, 0x6604)),
+                     lds(L.decBase + __byte_perm(w, L.laneWord, 0x6614)),
+                     lds(L.decBase + __byte_perm(w, L.laneWord, 0x6624)),
+                     lds(L.decBase + __byte_perm(w, L.laneWord, 0x6635)));
 }
 
-// Exact sRGB code of x (x >= 0, finite), returned in the low byte.
-//   z = max(269.025 x^(5/12) - 14.525, min(3294.6 x - 0.5, 9.8)) approximates
-//   255 * OETF(x) + 0.5 - 1 to ~1e-3, so a = rn(max(z, 0)) is code-1 or code;
-//   code = a + (x >= threshold[a]).  The magic add leaves a in the low bits
-//   of `bits`, and (bits << 7) + thrBase is the address of threshold[a].
+// Exact sRGB code of x in [0, 1], returned in the low byte.  With
+//   y  = 255 * OETF(x) + 0.5   (code = floor(y)),
+//   zp = 269.025 x^(5/12) - 14.925 = y - 1.4 on the power segment,
+//   zl = min(3294.6 x - 0.5, 9.4)  = y - 1   on the linear segment (capped),
+// z = max(zp, zl) lies in [y - 1.4, y - 1] up to ~1e-3, so a = rn(z) is code-1
+// or code, and code = a + (x >= threshold[a]).  z >= -0.5 (rounds to 0) and
+// z <= 254.1, so a indexes rows 0..254.  The magic add leaves a in the low
+// bits of `bits`, and (bits << 7) + thrBase is the address of threshold[a].
 __device__ __forceinline__ uint32_t encodeChannel(float x, const Lut& L) {
   const float p = ex2Approx(lg2Approx(x) * 0.41666666f);
-  const float zp = fmaf(p, 269.025f, -14.525f);
-  const float zl = fminf(fmaf(x, 3294.6f, -0.5f), 9.8f);
-  const float z = fmaxf(fmaxf(zp, zl), 0.0f);
-  const uint32_t bits = __float_as_uint(z + 12582912.0f);
-  const float thr = lutLoad(bits * 128u + L.thrBase);
+  const float zp = fmaf(p, 269.025f, -14.925f);
+  const float zl = fminf(fmaf(x, 3294.6f, -0.5f), 9.4f);
+  const uint32_t bits = __float_as_uint(fmaxf(zp, zl) + 12582912.0f);
+  const float thr = lds(bits * 128u + L.thrBase);
   return bits + (x >= thr ? 1u : 0u);
 }
 
@@ -176,118 +204,248 @@ __device__ __forceinline__ float4 shflDown(float4 v, int d) {
   return make_float4(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
                      __shfl_down_sync(0xffffffffu, v.z, d), __shfl_down_sync(0xffffffffu, v.w, d));
 }
-
-__device__ __forceinline__ float4 sel4(bool c, float4 a, float4 b) { return c ? a : b; }
-
-__device__ __forceinline__ void storeTexel(const FusedStage& st, uint32_t k, uint32_t x, uint32_t y, uint32_t v,
-                                           bool check) {
-  if (check && (x >= (st.coverW >> k) || y >= (st.coverH >> k))) return;
-  *reinterpret_cast<uint32_t*>(st.dst[k] + y * st.pitch[k] + uint64_t(x) * 4) = v;
+__device__ __forceinline__ float4 shflUp(float4 v, int d) {
+  return make_float4(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d),
+                     __shfl_up_sync(0xffffffffu, v.z, d), __shfl_up_sync(0xffffffffu, v.w, d));
 }
 
-// Levels L+1..L+N of one 64x64 region whose texels are in `tile` (shared).
-template <uint32_t N>
-__device__ __forceinline__ void processRegion(const FusedStage& st, uint32_t region, const uint32_t* tile,
-                                              float4* xchg, uint32_t g, uint32_t wig, uint32_t lane,
-                                              uint32_t iter, const Lut& L) {
-  const uint32_t x0 = (region % st.regionsX) * kTile, y0 = (region / st.regionsX) * kTile;
-  const bool check = x0 + kTile > st.coverW || y0 + kTile > st.coverH;
+__device__ __forceinline__ uint32_t* texelPtr(const FusedStage& st, uint32_t k, uint32_t x, uint32_t y) {
+  return reinterpret_cast<uint32_t*>(st.dst[k] + y * st.pitch[k] + uint64_t(x) * 4);
+}
+
+// Store texel (x, y) of level L+k; edge regions (CHECK) skip texels outside
+// the covered extent.
+template <bool CHECK>
+__device__ __forceinline__ void storeTexel(const FusedStage& st, uint32_t k, uint32_t x, uint32_t y, uint32_t v) {
+  if (CHECK && (x >= (st.coverW >> k) || y >= (st.coverH >> k))) return;
+  *texelPtr(st, k, x, y) = v;
+}
+
+// Levels L+1 and L+2 of a region from the buffer `tile`: the lane's four
+// level-(L+1) rows are built two at a time, each pair giving one level-(L+2)
+// texel (rows 4*wig + 2*half + j).  Level L+1 is stored as 8-byte pairs
+// (2cx, 2cx+1).  Returns the two level-(L+2) values.
+template <uint32_t N, bool CHECK>
+__device__ __forceinline__ void levels12(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
+                                         uint32_t wig, uint32_t lane, const Lut& L, float4& c0, float4& c1) {
   const uint32_t cx = lane & 15, half = lane >> 4;
-
-  // ---- level L+1 (vertical pairs first, LOAD_REDUCE4) ----
-  float4 a[4], b[4];
+  const uint32_t X = (x0 >> 1) + 2 * cx, Y0 = (y0 >> 1) + 8 * wig + 4 * half;
+  uint8_t* row = st.dst[1] + uint64_t(Y0) * st.pitch[1] + uint64_t(X) * 4;
+  const uint4* src = reinterpret_cast<const uint4*>(tile + (16 * wig + 8 * half) * kTile) + cx;
+  const bool inX = !CHECK || X < (st.coverW >> 1);  // X even, covered width even: pairs are whole
 #pragma unroll
-  for (uint32_t i = 0; i < 4; ++i) {
-    const uint32_t r0 = 16 * wig + 4 * i + 2 * half;
-    const uint4 t0 = reinterpret_cast<const uint4*>(tile + r0 * kTile)[cx];
-    const uint4 t1 = reinterpret_cast<const uint4*>(tile + (r0 + 1) * kTile)[cx];
-    a[i] = reduce4(decodeTexel(t0.x, L), decodeTexel(t1.x, L), decodeTexel(t0.y, L), decodeTexel(t1.y, L));
-    b[i] = reduce4(decodeTexel(t0.z, L), decodeTexel(t1.z, L), decodeTexel(t0.w, L), decodeTexel(t1.w, L));
-    const uint32_t ea = encodeTexel(a[i], L), eb = encodeTexel(b[i], L);
-    const uint32_t X = (x0 >> 1) + 2 * cx, Y = (y0 >> 1) + 8 * wig + 2 * i + half;
-    if (!check && st.l1Pairs) {
-      *reinterpret_cast<uint2*>(st.dst[1] + Y * st.pitch[1] + uint64_t(X) * 4) = make_uint2(ea, eb);
-    } else {
-      storeTexel(st, 1, X, Y, ea, check);
-      storeTexel(st, 1, X + 1, Y, eb, check);
-    }
-  }
-  if (N < 2) return;
-
-  // ---- level L+2: half 0 takes rows i = 0,1, half 1 rows i = 2,3 ----
-  float4 c[2];
-  {
-    const float4 s0a = shflXor(sel4(half, a[0], a[2]), 16), s0b = shflXor(sel4(half, b[0], b[2]), 16);
-    const float4 s1a = shflXor(sel4(half, a[1], a[3]), 16), s1b = shflXor(sel4(half, b[1], b[3]), 16);
-    const bool vert = fastVerticalFirst(N, 2);
-#pragma unroll
-    for (uint32_t j = 0; j < 2; ++j) {
-      const float4 ta = half ? (j ? s1a : s0a) : a[j], tb = half ? (j ? s1b : s0b) : b[j];
-      const float4 ba = half ? a[2 + j] : (j ? s1a : s0a), bb = half ? b[2 + j] : (j ? s1b : s0b);
-      c[j] = fastReduce(vert, ta, tb, ba, bb);
-      storeTexel(st, 2, (x0 >> 2) + cx, (y0 >> 2) + 4 * wig + 2 * half + j, encodeTexel(c[j], L), check);
-    }
-  }
-  if (N < 3) return;
-
-  // ---- level L+3: row 2*wig + half; right neighbour in lane + 1 ----
-  const float4 r0 = shflDown(c[0], 1), r1 = shflDown(c[1], 1);
-  const float4 d = fastReduce(fastVerticalFirst(N, 3), c[0], r0, c[1], r1);
-  if ((cx & 1) == 0)
-    storeTexel(st, 3, (x0 >> 3) + (cx >> 1), (y0 >> 3) + 2 * wig + half, encodeTexel(d, L), check);
-  if (N < 4) return;
-
-  // ---- level L+4: row wig from rows 2*wig (half 0) and 2*wig+1 (half 1) ----
-  const float4 e = shflXor(d, 16);
-  const float4 dr = shflDown(d, 2), er = shflDown(e, 2);
-  const float4 f = fastReduce(fastVerticalFirst(N, 4), d, dr, e, er);
-  if (half == 0 && (cx & 3) == 0) {
-    storeTexel(st, 4, (x0 >> 4) + (cx >> 2), (y0 >> 4) + wig, encodeTexel(f, L), check);
-    if (N >= 5) xchg[wig * 4 + (cx >> 2)] = f;
-  }
-  if (N < 5) return;
-
-  // ---- levels L+5, L+6 from the group's 4x4 block ----
-  groupSync(g);
-  if (wig == (iter & 3) && lane < 4) {
-    const uint32_t px = lane & 1, py = lane >> 1;
-    const float4 tl = xchg[(2 * py) * 4 + 2 * px], tr = xchg[(2 * py) * 4 + 2 * px + 1];
-    const float4 bl = xchg[(2 * py + 1) * 4 + 2 * px], br = xchg[(2 * py + 1) * 4 + 2 * px + 1];
-    const float4 v5 = fastReduce(fastVerticalFirst(N, 5), tl, tr, bl, br);
-    storeTexel(st, 5, (x0 >> 5) + px, (y0 >> 5) + py, encodeTexel(v5, L), check);
-    if (N >= 6) {
-      const float4 v1 = make_float4(__shfl_xor_sync(0xfu, v5.x, 1), __shfl_xor_sync(0xfu, v5.y, 1),
-                                    __shfl_xor_sync(0xfu, v5.z, 1), __shfl_xor_sync(0xfu, v5.w, 1));
-      const float4 v2 = make_float4(__shfl_xor_sync(0xfu, v5.x, 2), __shfl_xor_sync(0xfu, v5.y, 2),
-                                    __shfl_xor_sync(0xfu, v5.z, 2), __shfl_xor_sync(0xfu, v5.w, 2));
-      const float4 v3 = make_float4(__shfl_xor_sync(0xfu, v5.x, 3), __shfl_xor_sync(0xfu, v5.y, 3),
-                                    __shfl_xor_sync(0xfu, v5.z, 3), __shfl_xor_sync(0xfu, v5.w, 3));
-      if (lane == 0)
-        storeTexel(st, 6, x0 >> 6, y0 >> 6, encodeTexel(fastReduce(fastVerticalFirst(N, 6), v5, v1, v2, v3), L),
-                   check);
+  for (uint32_t j = 0; j < 2; ++j) {
+    const uint4 t0 = src[0], t1 = src[kTile / 4], t2 = src[2 * kTile / 4], t3 = src[3 * kTile / 4];
+    src += kTile;  // four rows of 64 texels
+    const float4 a0 = reduce4(decodeTexel(t0.x, L), decodeTexel(t1.x, L), decodeTexel(t0.y, L), decodeTexel(t1.y, L));
+    const float4 b0 = reduce4(decodeTexel(t0.z, L), decodeTexel(t1.z, L), decodeTexel(t0.w, L), decodeTexel(t1.w, L));
+    const float4 a1 = reduce4(decodeTexel(t2.x, L), decodeTexel(t3.x, L), decodeTexel(t2.y, L), decodeTexel(t3.y, L));
+    const float4 b1 = reduce4(decodeTexel(t2.z, L), decodeTexel(t3.z, L), decodeTexel(t2.w, L), decodeTexel(t3.w, L));
+    const uint2 e0 = make_uint2(encodeTexel(a0, L), encodeTexel(b0, L));
+    const uint2 e1 = make_uint2(encodeTexel(a1, L), encodeTexel(b1, L));
+    const uint32_t Y = Y0 + 2 * j;
+    if (!CHECK || (inX && Y < (st.coverH >> 1))) *reinterpret_cast<uint2*>(row) = e0;
+    if (!CHECK || (inX && Y + 1 < (st.coverH >> 1))) *reinterpret_cast<uint2*>(row + st.pitch[1]) = e1;
+    row += 2 * st.pitch[1];
+    if (N >= 2) {
+      const float4 c = fastReduce(fastVerticalFirst(N, 2), a0, b0, a1, b1);
+      storeTexel<CHECK>(st, 2, (x0 >> 2) + cx, (y0 >> 2) + 4 * wig + 2 * half + j, encodeTexel(c, L));
+      if (j == 0)
+        c0 = c;
+      else
+        c1 = c;
     }
   }
 }
 
-__device__ __forceinline__ void processRegionN(const FusedStage& st, uint32_t region, const uint32_t* tile,
-                                               float4* xchg, uint32_t g, uint32_t wig, uint32_t lane,
-                                               uint32_t iter, const Lut& L) {
+// Levels L+3 (row 2*wig + half, even cx) and L+4 (row wig, half 0,
+// cx % 4 == 0) from the level-(L+2) values, encoded in one pass: the
+// level-(L+4) value moves to the idle odd lane cx + 1, and each lane makes
+// at most one store.  For N >= 5 the level-(L+4) values go to `xchg`
+// ([row][col], 4x4).
+template <uint32_t N, bool CHECK>
+__device__ __forceinline__ void levels34(const FusedStage& st, uint32_t x0, uint32_t y0, float4 c0, float4 c1,
+                                         float4* xchg, uint32_t wig, uint32_t lane, const Lut& L) {
+  if (N < 3) return;
+  const uint32_t cx = lane & 15, half = lane >> 4;
+  const float4 r0 = shflDown(c0, 1), r1 = shflDown(c1, 1);
+  const float4 d = fastReduce(fastVerticalFirst(N, 3), c0, r0, c1, r1);
+  float4 v = d;
+  // this lane's output: level L+3 texel (even cx) or level L+4 texel (odd cx)
+  uint32_t k = 3, x = (x0 >> 3) + (cx >> 1), y = (y0 >> 3) + 2 * wig + half;
+  bool store = (cx & 1) == 0;
+  if (N >= 4) {
+    const float4 e = shflXor(d, 16);
+    const float4 dr = shflDown(d, 2), er = shflDown(e, 2);
+    const float4 f = fastReduce(fastVerticalFirst(N, 4), d, dr, e, er);
+    if (N >= 5 && half == 0 && (cx & 3) == 0) xchg[wig * 4 + (cx >> 2)] = f;
+    const float4 fu = shflUp(f, 1);
+    if (cx & 1) {
+      v = fu;
+      k = 4;
+      x = (x0 >> 4) + (cx >> 2);
+      y = (y0 >> 4) + wig;
+      store = half == 0 && (cx & 3) == 1;
+    }
+  }
+  const uint32_t code = encodeTexel(v, L);
+  if (store) storeTexel<CHECK>(st, k, x, y, code);
+}
+
+// Levels L+5 (and L+6) of a region from the group's 4x4 block in `xchg`,
+// by one warp: lanes 0..3 build level L+5, lane 4 receives level L+6; one
+// encode pass.
+template <uint32_t N, bool CHECK>
+__device__ __forceinline__ void finishTop(const FusedStage& st, uint32_t x0, uint32_t y0, const float4* xchg,
+                                          uint32_t lane, const Lut& L) {
+  if (N < 5 || lane >= 8) return;
+  const uint32_t px = lane & 1, py = (lane >> 1) & 1;
+  const float4 tl = xchg[(2 * py) * 4 + 2 * px], tr = xchg[(2 * py) * 4 + 2 * px + 1];
+  const float4 bl = xchg[(2 * py + 1) * 4 + 2 * px], br = xchg[(2 * py + 1) * 4 + 2 * px + 1];
+  float4 v = fastReduce(fastVerticalFirst(N, 5), tl, tr, bl, br);
+  if (N >= 6) {
+    constexpr uint32_t m = 0xffu;
+    const float4 v1 = make_float4(__shfl_xor_sync(m, v.x, 1), __shfl_xor_sync(m, v.y, 1),
+                                  __shfl_xor_sync(m, v.z, 1), __shfl_xor_sync(m, v.w, 1));
+    const float4 v2 = make_float4(__shfl_xor_sync(m, v.x, 2), __shfl_xor_sync(m, v.y, 2),
+                                  __shfl_xor_sync(m, v.z, 2), __shfl_xor_sync(m, v.w, 2));
+    const float4 v3 = make_float4(__shfl_xor_sync(m, v.x, 3), __shfl_xor_sync(m, v.y, 3),
+                                  __shfl_xor_sync(m, v.z, 3), __shfl_xor_sync(m, v.w, 3));
+    const float4 top = fastReduce(fastVerticalFirst(N, 6), v, v1, v2, v3);  // valid in lane 0
+    const float4 t4 = make_float4(__shfl_sync(m, top.x, 0), __shfl_sync(m, top.y, 0), __shfl_sync(m, top.z, 0),
+                                  __shfl_sync(m, top.w, 0));
+    if (lane == 4) v = t4;
+  }
+  if (lane > 4 || (N < 6 && lane == 4)) return;
+  const uint32_t code = encodeTexel(v, L);
+  if (lane < 4)
+    storeTexel<CHECK>(st, 5, (x0 >> 5) + px, (y0 >> 5) + py, code);
+  else
+    storeTexel<CHECK>(st, 6, x0 >> 6, y0 >> 6, code);
+}
+
+// Increment byte `slot` of a shared counter word on behalf of the warp;
+// true in every lane if this warp brought that byte to kGroupWarps (it is
+// then reset to 0).  The fences order the warp's earlier shared-memory
+// accesses before the count and the last warp's later ones after it.
+__device__ __forceinline__ bool lastWarpIn(uint32_t* word, uint32_t slot, uint32_t lane) {
+  __syncwarp();
+  uint32_t last = 0;
+  if (lane == 0) {
+    __threadfence_block();
+    const uint32_t old = atomicAdd(word, 1u << (8 * slot));
+    last = ((old >> (8 * slot)) & 0xffu) == kGroupWarps - 1;
+    if (last) {
+      atomicAnd(word, ~(0xffu << (8 * slot)));
+      __threadfence_block();
+    }
+  }
+  return __shfl_sync(0xffffffffu, last, 0) != 0;
+}
+
+struct GroupCtx {
+  const uint32_t* tiles;  // this group's region buffers
+  uint32_t stage0, bar0;  // shared addresses of this group's first buffer and mbarrier
+  uint32_t* relCnt;       // buffer-release counts (byte per buffer)
+  uint32_t* xchgCnt;      // exchange-deposit counts (byte per ring slot)
+  float4* xchg;           // this group's exchange ring
+};
+
+// One region of the main (TMA-fed) loop, barrier-free.  `next*` give the
+// region two steps ahead that goes into this region's buffer.
+template <uint32_t N, bool CHECK>
+__device__ __forceinline__ void mainRegion(const FusedStage& st, const CUtensorMap* map, const GroupCtx& G,
+                                           uint32_t x0, uint32_t y0, uint32_t s, uint32_t ring, bool hasNext,
+                                           uint32_t nextX, uint32_t nextY, uint32_t wig, uint32_t lane,
+                                           const Lut& L) {
+  const uint32_t* tile = G.tiles + s * (kTileBytes / 4);
+  float4 c0 = make_float4(0, 0, 0, 0), c1 = c0;
+  levels12<N, CHECK>(st, x0, y0, tile, wig, lane, L, c0, c1);
+  if (lastWarpIn(G.relCnt, s, lane) && hasNext && lane == 0)
+    tmaLoadRegion(G.stage0 + s * kTileBytes, map, nextX, nextY, G.bar0 + 8 * s);
+  float4* xchg = G.xchg + ring * 16;
+  levels34<N, CHECK>(st, x0, y0, c0, c1, xchg, wig, lane, L);
+  if (N >= 5 && lastWarpIn(G.xchgCnt, ring, lane)) finishTop<N, CHECK>(st, x0, y0, xchg, lane, L);
+}
+
+// One region of a tail dispatch: buffer filled with plain loads, group
+// barriers around the shared steps (the tail is a few regions at most).
+template <uint32_t N>
+__device__ __forceinline__ void tailRegion(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
+                                           float4* xchg, uint32_t g, uint32_t wig, uint32_t lane, uint32_t it,
+                                           const Lut& L) {
+  // the tail is a few regions: always bounds-checked
+  float4 c0 = make_float4(0, 0, 0, 0), c1 = c0;
+  levels12<N, true>(st, x0, y0, tile, wig, lane, L, c0, c1);
+  levels34<N, true>(st, x0, y0, c0, c1, xchg, wig, lane, L);
+  groupSync(g);
+  if (N >= 5 && wig == (it & 3)) finishTop<N, true>(st, x0, y0, xchg, lane, L);
+}
+
+template <uint32_t N>
+__device__ __forceinline__ bool mainLoop(const FusedStage& st, const CUtensorMap* map, const GroupCtx& G,
+                                         uint32_t gid, uint32_t groupsTotal, uint32_t wig, uint32_t lane,
+                                         const Lut& L) {
+  const uint32_t RX = st.regionsX, RY = st.regionsY;
+  const uint32_t dx1 = groupsTotal % RX, dy1 = groupsTotal / RX;
+  const uint32_t dx2 = (2 * groupsTotal) % RX, dy2 = (2 * groupsTotal) / RX;
+  uint32_t rx = gid % RX, ry = gid / RX;
+  uint32_t ring = 0;
+  for (uint32_t iter = 0; ry < RY; ++iter) {
+    const uint32_t s = iter & 1;
+    if (!mbarWait(G.bar0 + 8 * s, (iter >> 1) & 1)) return false;
+    uint32_t nx = rx + dx2, ny = ry + dy2;
+    if (nx >= RX) {
+      nx -= RX;
+      ++ny;
+    }
+    const uint32_t x0 = rx * kTile, y0 = ry * kTile;
+    if (x0 + kTile > st.coverW || y0 + kTile > st.coverH)
+      mainRegion<N, true>(st, map, G, x0, y0, s, ring, ny < RY, nx * kTile, ny * kTile, wig, lane, L);
+    else
+      mainRegion<N, false>(st, map, G, x0, y0, s, ring, ny < RY, nx * kTile, ny * kTile, wig, lane, L);
+    rx += dx1;
+    ry += dy1;
+    if (rx >= RX) {
+      rx -= RX;
+      ++ry;
+    }
+    ring = ring == kXchgRing - 1 ? 0 : ring + 1;
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool mainLoopN(const FusedStage& st, const CUtensorMap* map, const GroupCtx& G,
+                                          uint32_t gid, uint32_t groupsTotal, uint32_t wig, uint32_t lane,
+                                          const Lut& L) {
   switch (st.n) {
-    case 1: processRegion<1>(st, region, tile, xchg, g, wig, lane, iter, L); break;
-    case 2: processRegion<2>(st, region, tile, xchg, g, wig, lane, iter, L); break;
-    case 3: processRegion<3>(st, region, tile, xchg, g, wig, lane, iter, L); break;
-    case 4: processRegion<4>(st, region, tile, xchg, g, wig, lane, iter, L); break;
-    case 5: processRegion<5>(st, region, tile, xchg, g, wig, lane, iter, L); break;
-    default: processRegion<6>(st, region, tile, xchg, g, wig, lane, iter, L); break;
+    case 1: return mainLoop<1>(st, map, G, gid, groupsTotal, wig, lane, L);
+    case 2: return mainLoop<2>(st, map, G, gid, groupsTotal, wig, lane, L);
+    case 3: return mainLoop<3>(st, map, G, gid, groupsTotal, wig, lane, L);
+    case 4: return mainLoop<4>(st, map, G, gid, groupsTotal, wig, lane, L);
+    case 5: return mainLoop<5>(st, map, G, gid, groupsTotal, wig, lane, L);
+    default: return mainLoop<6>(st, map, G, gid, groupsTotal, wig, lane, L);
+  }
+}
+
+__device__ __forceinline__ void tailRegionN(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
+                                            float4* xchg, uint32_t g, uint32_t wig, uint32_t lane, uint32_t it,
+                                            const Lut& L) {
+  switch (st.n) {
+    case 1: tailRegion<1>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 2: tailRegion<2>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 3: tailRegion<3>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 4: tailRegion<4>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 5: tailRegion<5>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    default: tailRegion<6>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
   }
 }
 
 // Fill a region buffer from global memory with L2-coherent loads (tail
 // dispatches read a level written earlier in this kernel).  Texels outside
 // the covered extent are zero, as the TMA fill would give.
-__device__ __forceinline__ void loadRegionPlain(const FusedStage& st, uint32_t region, uint32_t* tile,
+__device__ __forceinline__ void loadRegionPlain(const FusedStage& st, uint32_t x0, uint32_t y0, uint32_t* tile,
                                                 uint32_t gtid) {
-  const uint32_t x0 = (region % st.regionsX) * kTile, y0 = (region / st.regionsX) * kTile;
   for (uint32_t i = gtid; i < kTile * kTile; i += kGroupThreads) {
     const uint32_t x = i % kTile, y = i / kTile;
     uint32_t v = 0;
@@ -302,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tmaFastKernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TmaParams p) {
   extern __shared__ __align__(128) uint8_t smem[];
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t g = warp >> 2, wig = warp & 3, gtid = tid & (kGroupThreads - 1);
+  const uint32_t g = warp / kGroupWarps, wig = warp % kGroupWarps, gtid = tid % kGroupThreads;
 
   float* lutDec = reinterpret_cast<float*>(smem + kLutDecodeOff);
   float* lutThr = reinterpret_cast<float*>(smem + kLutThrOff);
@@ -310,85 +468,69 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t code = i >> 5, l = i & 31;
     lutDec[code * 64 + l] = __uint_as_float(c_srgbDecodeBits[code]);
     lutDec[code * 64 + 32 + l] = __uint_as_float(c_alphaDecodeBits[code]);
-    lutThr[code * 32 + l] = __uint_as_float(c_srgbThresholdBits[code]);
+    if (code < kThrRows) lutThr[code * 32 + l] = __uint_as_float(c_srgbThresholdBits[code]);
   }
-  uint32_t* stage0 = reinterpret_cast<uint32_t*>(smem + kStageOff + (g * kStages + 0) * kTileBytes);
-  uint32_t* stage1 = reinterpret_cast<uint32_t*>(smem + kStageOff + (g * kStages + 1) * kTileBytes);
-  float4* xchgBase = reinterpret_cast<float4*>(smem + kXchgOff + g * 2 * 16 * 16);
-  const uint32_t bar0 = smemAddr(smem + kBarOff + (g * kStages + 0) * 8);
-  const uint32_t bar1 = bar0 + 8;
-  uint32_t* flags = reinterpret_cast<uint32_t*>(smem + kFlagOff);
+  GroupCtx G;
+  G.tiles = reinterpret_cast<const uint32_t*>(smem + kStageOff + g * kStages * kTileBytes);
+  G.stage0 = smemAddr(G.tiles);
+  G.bar0 = smemAddr(smem + kBarOff + g * kStages * 8);
+  G.relCnt = reinterpret_cast<uint32_t*>(smem + kCntOff) + 2 * g;
+  G.xchgCnt = G.relCnt + 1;
+  G.xchg = reinterpret_cast<float4*>(smem + kXchgOff) + g * kXchgRing * 16;
   if (gtid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar1) : "memory");
+    for (uint32_t s = 0; s < kStages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(G.bar0 + 8 * s) : "memory");
+    *G.relCnt = 0;
+    *G.xchgCnt = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-
-  Lut L;
-  L.laneWord = (4 * lane) | ((4 * lane + 128) << 8);
-  L.thrBase = kLutThrOff + 4 * lane - (0x4B400000u << 7);
+  const Lut L = makeLut(lane);
 
   const FusedStage& s0 = p.st[0];
   const uint32_t regions = s0.regionsX * s0.regionsY;
-  const uint32_t G = gridDim.x * kGroups;
+  const uint32_t groupsTotal = gridDim.x * kGroups;
   const uint32_t gid = g * gridDim.x + blockIdx.x;
   if (gtid == 0) {
     for (uint32_t s = 0; s < kStages; ++s) {
-      const uint32_t r = gid + s * G;
+      const uint32_t r = gid + s * groupsTotal;
       if (r < regions)
-        tmaLoadRegion(smemAddr(s ? stage1 : stage0), &tmap, (r % s0.regionsX) * kTile, (r / s0.regionsX) * kTile,
-                      s ? bar1 : bar0);
+        tmaLoadRegion(G.stage0 + s * kTileBytes, &tmap, (r % s0.regionsX) * kTile, (r / s0.regionsX) * kTile,
+                      G.bar0 + 8 * s);
     }
   }
-  bool ok = true;
-  uint32_t iter = 0;
-  for (;; ++iter) {
-    const uint32_t r = gid + iter * G;
-    if (r >= regions) break;
-    const uint32_t s = iter & 1;
-    if (!mbarWait(s ? bar1 : bar0, (iter >> 1) & 1)) {
-      ok = false;
-      break;
+  const bool ok = mainLoopN(s0, &tmap, G, gid, groupsTotal, wig, lane, L);
+  if (!ok && lane == 0) {
+    // A load never completed: record it and give every in-flight load of
+    // this group one more bounded wait before the CTA may exit.
+    atomicExch(p.errorFlag, 1u);
+    for (uint32_t s = 0; s < kStages; ++s) {
+      mbarWait(G.bar0 + 8 * s, 0);
+      mbarWait(G.bar0 + 8 * s, 1);
     }
-    processRegionN(s0, r, s ? stage1 : stage0, xchgBase + (iter & 1) * 16, g, wig, lane, iter, L);
-    groupSync(g);  // every warp is done with this buffer
-    const uint32_t rn = r + kStages * G;
-    if (gtid == 0 && rn < regions)
-      tmaLoadRegion(smemAddr(s ? stage1 : stage0), &tmap, (rn % s0.regionsX) * kTile, (rn / s0.regionsX) * kTile,
-                    s ? bar1 : bar0);
   }
-  if (!ok) {
-    // A load never completed: record it, drain the other buffer (bounded) and
-    // leave without touching the tail.
-    if (gtid == 0) atomicExch(p.errorFlag, 1u);
-    const uint32_t r1 = gid + (iter + 1) * G;
-    if (r1 < regions) mbarWait(((iter + 1) & 1) ? bar1 : bar0, ((iter + 1) >> 1) & 1);
-    return;
-  }
-  if (p.stageCount < 2) return;
+  if (__syncthreads_or(!ok) || p.stageCount < 2) return;
 
   // ---- last CTA runs the trailing dispatches ----
-  __syncthreads();
+  uint32_t last = 0;
   if (tid == 0) {
     __threadfence();
-    const uint32_t old = atomicAdd(p.counter, 1u);
-    const uint32_t last = old == gridDim.x - 1;
+    last = atomicAdd(p.counter, 1u) == gridDim.x - 1;
     if (last) {
       *p.counter = 0;
       __threadfence();
     }
-    flags[0] = last;
   }
-  __syncthreads();
-  if (!flags[0]) return;
+  if (!__syncthreads_or(last)) return;
+  uint32_t* tile = reinterpret_cast<uint32_t*>(smem + kStageOff + g * kStages * kTileBytes);
   for (uint32_t d = 1; d < p.stageCount; ++d) {
     const FusedStage& st = p.st[d];
     const uint32_t nreg = st.regionsX * st.regionsY;
     for (uint32_t r = g, it = 0; r < nreg; r += kGroups, ++it) {
-      loadRegionPlain(st, r, stage0, gtid);
+      const uint32_t x0 = (r % st.regionsX) * kTile, y0 = (r / st.regionsX) * kTile;
+      loadRegionPlain(st, x0, y0, tile, gtid);
       groupSync(g);
-      processRegionN(st, r, stage0, xchgBase + (it & 1) * 16, g, wig, lane, it, L);
+      tailRegionN(st, x0, y0, tile, G.xchg + (it % kXchgRing) * 16, g, wig, lane, it, L);
       groupSync(g);
     }
     __syncthreads();
@@ -399,23 +541,24 @@ __global__ void __launch_bounds__(kThreads, 1)
 __global__ void debugEncodeKernel(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n) {
   extern __shared__ __align__(128) uint8_t smem[];
   float* lutThr = reinterpret_cast<float*>(smem + kLutThrOff);
-  for (uint32_t i = threadIdx.x; i < 256 * 32; i += blockDim.x)
+  __shared__ float full[256];
+  for (uint32_t i = threadIdx.x; i < kThrRows * 32; i += blockDim.x)
     lutThr[i] = __uint_as_float(c_srgbThresholdBits[i >> 5]);
+  for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) full[i] = __uint_as_float(c_srgbThresholdBits[i]);
   __syncthreads();
-  Lut L;
-  L.laneWord = 0;
-  L.thrBase = kLutThrOff + 4 * (threadIdx.x & 31) - (0x4B400000u << 7);
+  const Lut L = makeLut(threadIdx.x & 31);
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += uint64_t(gridDim.x) * blockDim.x) {
     const float v = x[i];
-    fast[i] = uint8_t(encodeChannel(v, L));
+    // The fast encoder's table index is derived from the value; keep it in
+    // the encoder's domain [0, 1] (NaN -> 0) whatever the caller passes.
+    fast[i] = uint8_t(encodeChannel(fminf(fmaxf(v, 0.0f), 1.0f), L));
     uint32_t c = 0;  // the oracle's threshold count (binary search)
     for (uint32_t step = 128; step > 0; step >>= 1)
-      if (c + step <= 255 && lutThr[(c + step - 1) * 32] <= v) c += step;
+      if (c + step <= 255 && full[c + step - 1] <= v) c += step;
     exact[i] = uint8_t(c);
   }
 }
 
-// ---------------------------------------------------------------------------
 // Host side.
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -454,7 +597,8 @@ cudaError_t deviceInfo(DeviceInfo** out) {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(tmaFastKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(debugEncodeKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
+      e = cudaFuncSetAttribute(debugEncodeKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(kDebugSmemBytes));
     if (e != cudaSuccess) return e;
     d.configured = true;
   }
@@ -476,7 +620,6 @@ void fillStage(const DispatchParams& p, FusedStage* st) {
   st->coverH = (p.lv[0].h >> n) << n;
   st->regionsX = (st->coverW + kTile - 1) / kTile;
   st->regionsY = (st->coverH + kTile - 1) / kTile;
-  st->l1Pairs = (reinterpret_cast<uintptr_t>(p.lv[1].ptr) % 8 == 0) && (p.lv[1].pitch % 8 == 0);
   st->src = p.lv[0].ptr;
   st->srcPitch = p.lv[0].pitch;
   for (uint32_t k = 0; k <= kMaxDispatchLevels; ++k) {
@@ -492,6 +635,9 @@ bool tmaFastSupported(const DispatchParams& p) {
   const LevelView& v = p.lv[0];
   if (reinterpret_cast<uintptr_t>(v.ptr) % 16 || v.pitch % 16 || v.pitch >= (uint64_t(1) << 40)) return false;
   if ((v.w >> p.levelCount) == 0 || (v.h >> p.levelCount) == 0) return false;
+  // 8-byte level-(L+1) pairs: aligned, and whole at the right edge
+  if (reinterpret_cast<uintptr_t>(p.lv[1].ptr) % 8 || p.lv[1].pitch % 8 || ((v.w >> p.levelCount) << p.levelCount) % 4)
+    return false;
   if (p.groups < fastGroupsNeeded(p)) return false;  // partial grids: portable kernel
   return encodeTiled() != nullptr;
 }
@@ -502,6 +648,9 @@ bool tmaTailCompatible(const DispatchParams& prev, const DispatchParams& next) {
   if (next.lv[0].ptr != prev.lv[prev.levelCount].ptr || next.lv[0].pitch != prev.lv[prev.levelCount].pitch)
     return false;
   if ((next.lv[0].w >> next.levelCount) == 0 || (next.lv[0].h >> next.levelCount) == 0) return false;
+  if (reinterpret_cast<uintptr_t>(next.lv[1].ptr) % 8 || next.lv[1].pitch % 8 ||
+      ((next.lv[0].w >> next.levelCount) << next.levelCount) % 4)
+    return false;
   if (next.groups < fastGroupsNeeded(next)) return false;
   // one CTA runs the tail: keep it to a few regions
   return uint64_t(next.lv[0].w) * next.lv[0].h <= 256u * 256u;
@@ -542,7 +691,7 @@ cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uin
   DeviceInfo* info = nullptr;
   cudaError_t e = deviceInfo(&info);
   if (e != cudaSuccess) return e;
-  debugEncodeKernel<<<info->sms * 2, 256, kSmemBytes, stream>>>(x, fast, exact, n);
+  debugEncodeKernel<<<info->sms * 2, 256, kDebugSmemBytes, stream>>>(x, fast, exact, n);
   return cudaGetLastError();
 }
 
