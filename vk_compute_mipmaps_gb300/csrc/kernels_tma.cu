@@ -18,13 +18,13 @@
 // The operand order of every REDUCE4 follows fastVerticalFirst(n, k), so the
 // bytes equal the portable kernel's and the CPU oracle's.
 //
-// No group barrier in the steady state.  The last warp to finish reading a
-// region buffer (a shared-memory atomic count) issues the TMA for the
-// group's region two steps ahead into it; the last warp to deposit its
-// level-(L+4) values finishes levels L+5/L+6.  The exchange buffers form a
-// ring of three: a warp can be at most two regions ahead of the slowest one,
-// because the load of region i+2 waits for every warp to leave region i's
-// buffer.
+// Producer warps.  Each group has a producer warp.  For each region i of
+// its group it waits on the "buffer empty" mbarrier (four warp arrivals after
+// their level-(L+1) reads) and issues the TMA of region i+2 into the buffer;
+// then it waits on the "exchange full" mbarrier (four arrivals after the
+// level-(L+4) deposits), finishes levels L+5/L+6 and arrives on the slot's
+// "exchange empty" mbarrier, which the group waits on before depositing into
+// that slot again (region i+2).  Consumer warps never wait on each other.
 //
 // sRGB codec.  Decode is a table lookup per channel from a table replicated
 // once per lane (row c holds 32 copies of decode[c] then 32 of alpha[c]), so
@@ -53,13 +53,18 @@ constexpr uint32_t kTile = 64;
 constexpr uint32_t kGroups = 4;
 constexpr uint32_t kGroupWarps = 4;
 constexpr uint32_t kGroupThreads = kGroupWarps * 32;
-constexpr uint32_t kThreads = kGroups * kGroupThreads;
+constexpr uint32_t kConsumerThreads = kGroups * kGroupThreads;
+constexpr uint32_t kProducerWarp0 = kConsumerThreads / 32;  // one producer warp per group
+constexpr uint32_t kThreads = kConsumerThreads + 32 * kGroups;
 constexpr uint32_t kStages = 2;
-constexpr uint32_t kXchgRing = 3;
+constexpr uint32_t kXchgRing = 2;
 constexpr uint32_t kTileBytes = kTile * kTile * 4;
 constexpr uint32_t kMaxFused = 4;
-constexpr uint32_t kWaitLimit = 1u << 16;  // bounded mbarrier polling ...
-constexpr uint32_t kWaitHintNs = 20000;    // ... of at most ~20 us each
+// Bounded mbarrier waits: a failed poll backs off with nanosleep so that
+// waiting warps do not take issue slots from working ones; after
+// kWaitLimit polls (about a second) the wait gives up and reports it.
+constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr uint32_t kWaitBackoffNs = 128;
 
 // Byte offsets inside the dynamic shared memory block.
 constexpr uint32_t kLutDecodeOff = 0;                          // 256 rows x 256 B
@@ -67,9 +72,10 @@ constexpr uint32_t kThrRows = 255;                             // candidates sta
 constexpr uint32_t kLutThrOff = kLutDecodeOff + 256 * 256;     // 255 rows x 128 B
 constexpr uint32_t kStageOff = kLutThrOff + kThrRows * 128;    // [group][stage] x 16 KiB
 constexpr uint32_t kXchgOff = kStageOff + kGroups * kStages * kTileBytes;  // [group][ring][16] float4
-constexpr uint32_t kBarOff = kXchgOff + kGroups * kXchgRing * 16 * 16;     // [group][stage] mbarrier
-constexpr uint32_t kCntOff = kBarOff + kGroups * kStages * 8;              // [group] release, exchange
-constexpr uint32_t kSmemBytes = kCntOff + kGroups * 2 * 4;
+constexpr uint32_t kBarOff = kXchgOff + kGroups * kXchgRing * 16 * 16;     // mbarriers, per group:
+// full[stage], empty[stage], xfull[ring], xempty[ring]
+constexpr uint32_t kBarsPerGroup = 2 * kStages + 2 * kXchgRing;
+constexpr uint32_t kSmemBytes = kBarOff + kGroups * kBarsPerGroup * 8;
 static_assert(kStageOff % 128 == 0, "TMA destinations need 128-byte alignment");
 static_assert(kSmemBytes <= 232448, "exceeds the 227 KiB of shared memory per CTA");
 constexpr uint32_t kDebugSmemBytes = kLutThrOff + kThrRows * 128;
@@ -103,13 +109,18 @@ __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
   for (uint32_t it = 0; it < kWaitLimit; ++it) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(bar), "r"(parity), "r"(kWaitHintNs)
+        : "r"(bar), "r"(parity)
         : "memory");
     if (done) return true;
+    __nanosleep(kWaitBackoffNs);
   }
   return false;
+}
+
+__device__ __forceinline__ void mbarArrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ void tmaLoadRegion(uint32_t dst, const CUtensorMap* map, uint32_t x, uint32_t y,
@@ -190,10 +201,47 @@ __device__ __forceinline__ uint32_t encodeAlpha(float a) {
   return __float_as_uint(__fadd_rz(s, 8388608.0f));
 }
 
+// encodeChannel x3 + encodeAlpha with the independent multiplies and adds
+// paired into packed FP32 instructions (each lane of __fmul2_rn/__fadd2_rn/
+// __ffma2_rn rounds exactly like its scalar form, so the bytes are those of
+// the scalar functions).
 __device__ __forceinline__ uint32_t encodeTexel(float4 v, const Lut& L) {
-  const uint32_t r = encodeChannel(v.x, L), g = encodeChannel(v.y, L), b = encodeChannel(v.z, L);
-  const uint32_t a = encodeAlpha(v.w);
+  constexpr float k = 0.41666666f, magic = 12582912.0f;
+  const float2 tRG = __fmul2_rn(make_float2(lg2Approx(v.x), lg2Approx(v.y)), make_float2(k, k));
+  const float2 tBa = __fmul2_rn(make_float2(lg2Approx(v.z), v.w), make_float2(k, 255.0f));  // (tB, a*255)
+  const float2 pRG = make_float2(ex2Approx(tRG.x), ex2Approx(tRG.y));
+  const float pB = ex2Approx(tBa.x);
+  const float2 zpRG = __ffma2_rn(pRG, make_float2(269.025f, 269.025f), make_float2(-14.925f, -14.925f));
+  // (zpB, a*255 + 0.5): the alpha add is exact-as-written (a*255*1 is exact)
+  const float2 zpBs = __ffma2_rn(make_float2(pB, tBa.y), make_float2(269.025f, 1.0f), make_float2(-14.925f, 0.5f));
+  const float2 zlRG = __ffma2_rn(make_float2(v.x, v.y), make_float2(3294.6f, 3294.6f), make_float2(-0.5f, -0.5f));
+  const float zlB = fmaf(v.z, 3294.6f, -0.5f);
+  const float2 mRG = __fadd2_rn(make_float2(fmaxf(zpRG.x, fminf(zlRG.x, 9.4f)), fmaxf(zpRG.y, fminf(zlRG.y, 9.4f))),
+                                make_float2(magic, magic));
+  const uint32_t bR = __float_as_uint(mRG.x), bG = __float_as_uint(mRG.y);
+  const uint32_t bB = __float_as_uint(fmaxf(zpBs.x, fminf(zlB, 9.4f)) + magic);
+  const uint32_t r = bR + (v.x >= lds(bR * 128u + L.thrBase) ? 1u : 0u);
+  const uint32_t g = bG + (v.y >= lds(bG * 128u + L.thrBase) ? 1u : 0u);
+  const uint32_t b = bB + (v.z >= lds(bB * 128u + L.thrBase) ? 1u : 0u);
+  const uint32_t a = __float_as_uint(__fadd_rz(zpBs.y, 8388608.0f));
   return __byte_perm(__byte_perm(r, g, 0x0040), __byte_perm(b, a, 0x0040), 0x5410);
+}
+
+// REDUCE4 on packed pairs: 0.25 * ((v00 + v01) + (v10 + v11)) per channel,
+// same operations and order as reduce4().
+__device__ __forceinline__ float4 add4p(float4 a, float4 b) {
+  const float2 lo = __fadd2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
+  const float2 hi = __fadd2_rn(make_float2(a.z, a.w), make_float2(b.z, b.w));
+  return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+__device__ __forceinline__ float4 reduce4p(float4 v00, float4 v01, float4 v10, float4 v11) {
+  const float4 t = add4p(add4p(v00, v01), add4p(v10, v11));
+  const float2 lo = __fmul2_rn(make_float2(0.25f, 0.25f), make_float2(t.x, t.y));
+  const float2 hi = __fmul2_rn(make_float2(0.25f, 0.25f), make_float2(t.z, t.w));
+  return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+__device__ __forceinline__ float4 fastReduceP(bool vertical, float4 tl, float4 tr, float4 bl, float4 br) {
+  return vertical ? reduce4p(tl, bl, tr, br) : reduce4p(tl, tr, bl, br);
 }
 
 __device__ __forceinline__ float4 shflXor(float4 v, int m) {
@@ -237,10 +285,10 @@ __device__ __forceinline__ void levels12(const FusedStage& st, uint32_t x0, uint
   for (uint32_t j = 0; j < 2; ++j) {
     const uint4 t0 = src[0], t1 = src[kTile / 4], t2 = src[2 * kTile / 4], t3 = src[3 * kTile / 4];
     src += kTile;  // four rows of 64 texels
-    const float4 a0 = reduce4(decodeTexel(t0.x, L), decodeTexel(t1.x, L), decodeTexel(t0.y, L), decodeTexel(t1.y, L));
-    const float4 b0 = reduce4(decodeTexel(t0.z, L), decodeTexel(t1.z, L), decodeTexel(t0.w, L), decodeTexel(t1.w, L));
-    const float4 a1 = reduce4(decodeTexel(t2.x, L), decodeTexel(t3.x, L), decodeTexel(t2.y, L), decodeTexel(t3.y, L));
-    const float4 b1 = reduce4(decodeTexel(t2.z, L), decodeTexel(t3.z, L), decodeTexel(t2.w, L), decodeTexel(t3.w, L));
+    const float4 a0 = reduce4p(decodeTexel(t0.x, L), decodeTexel(t1.x, L), decodeTexel(t0.y, L), decodeTexel(t1.y, L));
+    const float4 b0 = reduce4p(decodeTexel(t0.z, L), decodeTexel(t1.z, L), decodeTexel(t0.w, L), decodeTexel(t1.w, L));
+    const float4 a1 = reduce4p(decodeTexel(t2.x, L), decodeTexel(t3.x, L), decodeTexel(t2.y, L), decodeTexel(t3.y, L));
+    const float4 b1 = reduce4p(decodeTexel(t2.z, L), decodeTexel(t3.z, L), decodeTexel(t2.w, L), decodeTexel(t3.w, L));
     const uint2 e0 = make_uint2(encodeTexel(a0, L), encodeTexel(b0, L));
     const uint2 e1 = make_uint2(encodeTexel(a1, L), encodeTexel(b1, L));
     const uint32_t Y = Y0 + 2 * j;
@@ -248,7 +296,7 @@ __device__ __forceinline__ void levels12(const FusedStage& st, uint32_t x0, uint
     if (!CHECK || (inX && Y + 1 < (st.coverH >> 1))) *reinterpret_cast<uint2*>(row + st.pitch[1]) = e1;
     row += 2 * st.pitch[1];
     if (N >= 2) {
-      const float4 c = fastReduce(fastVerticalFirst(N, 2), a0, b0, a1, b1);
+      const float4 c = fastReduceP(fastVerticalFirst(N, 2), a0, b0, a1, b1);
       storeTexel<CHECK>(st, 2, (x0 >> 2) + cx, (y0 >> 2) + 4 * wig + 2 * half + j, encodeTexel(c, L));
       if (j == 0)
         c0 = c;
@@ -269,7 +317,7 @@ __device__ __forceinline__ void levels34(const FusedStage& st, uint32_t x0, uint
   if (N < 3) return;
   const uint32_t cx = lane & 15, half = lane >> 4;
   const float4 r0 = shflDown(c0, 1), r1 = shflDown(c1, 1);
-  const float4 d = fastReduce(fastVerticalFirst(N, 3), c0, r0, c1, r1);
+  const float4 d = fastReduceP(fastVerticalFirst(N, 3), c0, r0, c1, r1);
   float4 v = d;
   // this lane's output: level L+3 texel (even cx) or level L+4 texel (odd cx)
   uint32_t k = 3, x = (x0 >> 3) + (cx >> 1), y = (y0 >> 3) + 2 * wig + half;
@@ -277,7 +325,7 @@ __device__ __forceinline__ void levels34(const FusedStage& st, uint32_t x0, uint
   if (N >= 4) {
     const float4 e = shflXor(d, 16);
     const float4 dr = shflDown(d, 2), er = shflDown(e, 2);
-    const float4 f = fastReduce(fastVerticalFirst(N, 4), d, dr, e, er);
+    const float4 f = fastReduceP(fastVerticalFirst(N, 4), d, dr, e, er);
     if (N >= 5 && half == 0 && (cx & 3) == 0) xchg[wig * 4 + (cx >> 2)] = f;
     const float4 fu = shflUp(f, 1);
     if (cx & 1) {
@@ -302,7 +350,7 @@ __device__ __forceinline__ void finishTop(const FusedStage& st, uint32_t x0, uin
   const uint32_t px = lane & 1, py = (lane >> 1) & 1;
   const float4 tl = xchg[(2 * py) * 4 + 2 * px], tr = xchg[(2 * py) * 4 + 2 * px + 1];
   const float4 bl = xchg[(2 * py + 1) * 4 + 2 * px], br = xchg[(2 * py + 1) * 4 + 2 * px + 1];
-  float4 v = fastReduce(fastVerticalFirst(N, 5), tl, tr, bl, br);
+  float4 v = fastReduceP(fastVerticalFirst(N, 5), tl, tr, bl, br);
   if (N >= 6) {
     constexpr uint32_t m = 0xffu;
     const float4 v1 = make_float4(__shfl_xor_sync(m, v.x, 1), __shfl_xor_sync(m, v.y, 1),
@@ -311,7 +359,7 @@ __device__ __forceinline__ void finishTop(const FusedStage& st, uint32_t x0, uin
                                   __shfl_xor_sync(m, v.z, 2), __shfl_xor_sync(m, v.w, 2));
     const float4 v3 = make_float4(__shfl_xor_sync(m, v.x, 3), __shfl_xor_sync(m, v.y, 3),
                                   __shfl_xor_sync(m, v.z, 3), __shfl_xor_sync(m, v.w, 3));
-    const float4 top = fastReduce(fastVerticalFirst(N, 6), v, v1, v2, v3);  // valid in lane 0
+    const float4 top = fastReduceP(fastVerticalFirst(N, 6), v, v1, v2, v3);  // valid in lane 0
     const float4 t4 = make_float4(__shfl_sync(m, top.x, 0), __shfl_sync(m, top.y, 0), __shfl_sync(m, top.z, 0),
                                   __shfl_sync(m, top.w, 0));
     if (lane == 4) v = t4;
@@ -324,48 +372,138 @@ __device__ __forceinline__ void finishTop(const FusedStage& st, uint32_t x0, uin
     storeTexel<CHECK>(st, 6, x0 >> 6, y0 >> 6, code);
 }
 
-// Increment byte `slot` of a shared counter word on behalf of the warp;
-// true in every lane if this warp brought that byte to kGroupWarps (it is
-// then reset to 0).  The fences order the warp's earlier shared-memory
-// accesses before the count and the last warp's later ones after it.
-__device__ __forceinline__ bool lastWarpIn(uint32_t* word, uint32_t slot, uint32_t lane) {
-  __syncwarp();
-  uint32_t last = 0;
-  if (lane == 0) {
-    __threadfence_block();
-    const uint32_t old = atomicAdd(word, 1u << (8 * slot));
-    last = ((old >> (8 * slot)) & 0xffu) == kGroupWarps - 1;
-    if (last) {
-      atomicAnd(word, ~(0xffu << (8 * slot)));
-      __threadfence_block();
-    }
-  }
-  return __shfl_sync(0xffffffffu, last, 0) != 0;
-}
-
 struct GroupCtx {
   const uint32_t* tiles;  // this group's region buffers
-  uint32_t stage0, bar0;  // shared addresses of this group's first buffer and mbarrier
-  uint32_t* relCnt;       // buffer-release counts (byte per buffer)
-  uint32_t* xchgCnt;      // exchange-deposit counts (byte per ring slot)
+  uint32_t stage0;        // shared address of its first buffer
+  uint32_t full0;         // mbarriers: full[stage], empty[stage], xfull[ring]
+  uint32_t empty0;
+  uint32_t xfull0;
+  uint32_t xempty0;
   float4* xchg;           // this group's exchange ring
 };
 
-// One region of the main (TMA-fed) loop, barrier-free.  `next*` give the
-// region two steps ahead that goes into this region's buffer.
+__device__ __forceinline__ GroupCtx groupCtx(uint32_t g) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  GroupCtx G;
+  G.tiles = reinterpret_cast<const uint32_t*>(smem + kStageOff + g * kStages * kTileBytes);
+  G.stage0 = smemAddr(G.tiles);
+  G.full0 = smemAddr(smem + kBarOff + g * kBarsPerGroup * 8);
+  G.empty0 = G.full0 + 8 * kStages;
+  G.xfull0 = G.empty0 + 8 * kStages;
+  G.xempty0 = G.xfull0 + 8 * kXchgRing;
+  G.xchg = reinterpret_cast<float4*>(smem + kXchgOff) + g * kXchgRing * 16;
+  return G;
+}
+
+// One region of the main (TMA-fed) loop for a consumer warp.
 template <uint32_t N, bool CHECK>
-__device__ __forceinline__ void mainRegion(const FusedStage& st, const CUtensorMap* map, const GroupCtx& G,
-                                           uint32_t x0, uint32_t y0, uint32_t s, uint32_t ring, bool hasNext,
-                                           uint32_t nextX, uint32_t nextY, uint32_t wig, uint32_t lane,
-                                           const Lut& L) {
+__device__ __forceinline__ bool mainRegion(const FusedStage& st, const GroupCtx& G, uint32_t x0, uint32_t y0,
+                                           uint32_t iter, uint32_t wig, uint32_t lane, const Lut& L) {
+  const uint32_t s = iter & 1, ring = iter & 1;
   const uint32_t* tile = G.tiles + s * (kTileBytes / 4);
   float4 c0 = make_float4(0, 0, 0, 0), c1 = c0;
   levels12<N, CHECK>(st, x0, y0, tile, wig, lane, L, c0, c1);
-  if (lastWarpIn(G.relCnt, s, lane) && hasNext && lane == 0)
-    tmaLoadRegion(G.stage0 + s * kTileBytes, map, nextX, nextY, G.bar0 + 8 * s);
-  float4* xchg = G.xchg + ring * 16;
-  levels34<N, CHECK>(st, x0, y0, c0, c1, xchg, wig, lane, L);
-  if (N >= 5 && lastWarpIn(G.xchgCnt, ring, lane)) finishTop<N, CHECK>(st, x0, y0, xchg, lane, L);
+  __syncwarp();
+  if (lane == 0) mbarArrive(G.empty0 + 8 * s);  // this warp is done with the buffer
+  // before depositing into this exchange slot again, the producer must have
+  // finished the region that used it two steps ago
+  if (N >= 5 && iter >= 2 && !mbarWait(G.xempty0 + 8 * ring, ((iter >> 1) - 1) & 1)) return false;
+  levels34<N, CHECK>(st, x0, y0, c0, c1, G.xchg + ring * 16, wig, lane, L);
+  if (N >= 5) {
+    __syncwarp();
+    if (lane == 0) mbarArrive(G.xfull0 + 8 * ring);  // its part of the 4x4 block is deposited
+  }
+  return true;
+}
+
+// Region coordinates (in regions) of a group's i-th region, advanced by the
+// stride of all groups without divisions.
+struct RegionCursor {
+  uint32_t rx, ry, dx, dy, RX;
+  __device__ __forceinline__ RegionCursor(uint32_t first, uint32_t stride, uint32_t regionsX)
+      : rx(first % regionsX), ry(first / regionsX), dx(stride % regionsX), dy(stride / regionsX), RX(regionsX) {}
+  __device__ __forceinline__ void next() {
+    rx += dx;
+    ry += dy;
+    if (rx >= RX) {
+      rx -= RX;
+      ++ry;
+    }
+  }
+};
+
+template <uint32_t N>
+__device__ __forceinline__ bool consumerLoop(const FusedStage& st, const GroupCtx& G, uint32_t gid,
+                                             uint32_t groupsTotal, uint32_t wig, uint32_t lane, const Lut& L) {
+  RegionCursor c(gid, groupsTotal, st.regionsX);
+  for (uint32_t iter = 0; c.ry < st.regionsY; ++iter, c.next()) {
+    const uint32_t s = iter & 1;
+    if (!mbarWait(G.full0 + 8 * s, (iter >> 1) & 1)) return false;
+    const uint32_t x0 = c.rx * kTile, y0 = c.ry * kTile;
+    const bool ok = (x0 + kTile > st.coverW || y0 + kTile > st.coverH)
+                        ? mainRegion<N, true>(st, G, x0, y0, iter, wig, lane, L)
+                        : mainRegion<N, false>(st, G, x0, y0, iter, wig, lane, L);
+    if (!ok) return false;
+  }
+  return true;
+}
+
+// The producer warp of group g: refill region i's buffer with region i+2 as
+// soon as it is empty, then finish levels L+5/L+6 of region i.
+template <uint32_t N>
+__device__ __forceinline__ bool producerLoop(const FusedStage& st, const CUtensorMap* map, const GroupCtx& G,
+                                             uint32_t gid, uint32_t groupsTotal, uint32_t lane, const Lut& L) {
+  RegionCursor cur(gid, groupsTotal, st.regionsX);
+  RegionCursor ahead = cur;
+  ahead.next();
+  ahead.next();
+  for (uint32_t iter = 0; cur.ry < st.regionsY; ++iter, cur.next(), ahead.next()) {
+    const uint32_t s = iter & 1, parity = (iter >> 1) & 1;
+    if (ahead.ry < st.regionsY) {
+      if (!mbarWait(G.empty0 + 8 * s, parity)) return false;
+      if (lane == 0)
+        tmaLoadRegion(G.stage0 + s * kTileBytes, map, ahead.rx * kTile, ahead.ry * kTile, G.full0 + 8 * s);
+    }
+    if (N >= 5) {
+      if (!mbarWait(G.xfull0 + 8 * s, parity)) return false;
+      const uint32_t x0 = cur.rx * kTile, y0 = cur.ry * kTile;
+      if (x0 + kTile > st.coverW || y0 + kTile > st.coverH)
+        finishTop<N, true>(st, x0, y0, G.xchg + s * 16, lane, L);
+      else
+        finishTop<N, false>(st, x0, y0, G.xchg + s * 16, lane, L);
+      __syncwarp();
+      if (lane == 0) mbarArrive(G.xempty0 + 8 * s);  // the slot may be reused
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool mainLoopN(const FusedStage& st, const CUtensorMap* map, uint32_t warp,
+                                          uint32_t groupsTotal, uint32_t lane, const Lut& L) {
+  if (warp >= kProducerWarp0) {
+    const uint32_t g = warp - kProducerWarp0;
+    const GroupCtx G = groupCtx(g);
+    const uint32_t gid = g * gridDim.x + blockIdx.x;
+    switch (st.n) {
+      case 1: return producerLoop<1>(st, map, G, gid, groupsTotal, lane, L);
+      case 2: return producerLoop<2>(st, map, G, gid, groupsTotal, lane, L);
+      case 3: return producerLoop<3>(st, map, G, gid, groupsTotal, lane, L);
+      case 4: return producerLoop<4>(st, map, G, gid, groupsTotal, lane, L);
+      case 5: return producerLoop<5>(st, map, G, gid, groupsTotal, lane, L);
+      default: return producerLoop<6>(st, map, G, gid, groupsTotal, lane, L);
+    }
+  }
+  const uint32_t g = warp / kGroupWarps, wig = warp % kGroupWarps;
+  const GroupCtx G = groupCtx(g);
+  const uint32_t gid = g * gridDim.x + blockIdx.x;
+  switch (st.n) {
+    case 1: return consumerLoop<1>(st, G, gid, groupsTotal, wig, lane, L);
+    case 2: return consumerLoop<2>(st, G, gid, groupsTotal, wig, lane, L);
+    case 3: return consumerLoop<3>(st, G, gid, groupsTotal, wig, lane, L);
+    case 4: return consumerLoop<4>(st, G, gid, groupsTotal, wig, lane, L);
+    case 5: return consumerLoop<5>(st, G, gid, groupsTotal, wig, lane, L);
+    default: return consumerLoop<6>(st, G, gid, groupsTotal, wig, lane, L);
+  }
 }
 
 // One region of a tail dispatch: buffer filled with plain loads, group
@@ -380,52 +518,6 @@ __device__ __forceinline__ void tailRegion(const FusedStage& st, uint32_t x0, ui
   levels34<N, true>(st, x0, y0, c0, c1, xchg, wig, lane, L);
   groupSync(g);
   if (N >= 5 && wig == (it & 3)) finishTop<N, true>(st, x0, y0, xchg, lane, L);
-}
-
-template <uint32_t N>
-__device__ __forceinline__ bool mainLoop(const FusedStage& st, const CUtensorMap* map, const GroupCtx& G,
-                                         uint32_t gid, uint32_t groupsTotal, uint32_t wig, uint32_t lane,
-                                         const Lut& L) {
-  const uint32_t RX = st.regionsX, RY = st.regionsY;
-  const uint32_t dx1 = groupsTotal % RX, dy1 = groupsTotal / RX;
-  const uint32_t dx2 = (2 * groupsTotal) % RX, dy2 = (2 * groupsTotal) / RX;
-  uint32_t rx = gid % RX, ry = gid / RX;
-  uint32_t ring = 0;
-  for (uint32_t iter = 0; ry < RY; ++iter) {
-    const uint32_t s = iter & 1;
-    if (!mbarWait(G.bar0 + 8 * s, (iter >> 1) & 1)) return false;
-    uint32_t nx = rx + dx2, ny = ry + dy2;
-    if (nx >= RX) {
-      nx -= RX;
-      ++ny;
-    }
-    const uint32_t x0 = rx * kTile, y0 = ry * kTile;
-    if (x0 + kTile > st.coverW || y0 + kTile > st.coverH)
-      mainRegion<N, true>(st, map, G, x0, y0, s, ring, ny < RY, nx * kTile, ny * kTile, wig, lane, L);
-    else
-      mainRegion<N, false>(st, map, G, x0, y0, s, ring, ny < RY, nx * kTile, ny * kTile, wig, lane, L);
-    rx += dx1;
-    ry += dy1;
-    if (rx >= RX) {
-      rx -= RX;
-      ++ry;
-    }
-    ring = ring == kXchgRing - 1 ? 0 : ring + 1;
-  }
-  return true;
-}
-
-__device__ __forceinline__ bool mainLoopN(const FusedStage& st, const CUtensorMap* map, const GroupCtx& G,
-                                          uint32_t gid, uint32_t groupsTotal, uint32_t wig, uint32_t lane,
-                                          const Lut& L) {
-  switch (st.n) {
-    case 1: return mainLoop<1>(st, map, G, gid, groupsTotal, wig, lane, L);
-    case 2: return mainLoop<2>(st, map, G, gid, groupsTotal, wig, lane, L);
-    case 3: return mainLoop<3>(st, map, G, gid, groupsTotal, wig, lane, L);
-    case 4: return mainLoop<4>(st, map, G, gid, groupsTotal, wig, lane, L);
-    case 5: return mainLoop<5>(st, map, G, gid, groupsTotal, wig, lane, L);
-    default: return mainLoop<6>(st, map, G, gid, groupsTotal, wig, lane, L);
-  }
 }
 
 __device__ __forceinline__ void tailRegionN(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
@@ -460,7 +552,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     tmaFastKernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TmaParams p) {
   extern __shared__ __align__(128) uint8_t smem[];
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t g = warp / kGroupWarps, wig = warp % kGroupWarps, gtid = tid % kGroupThreads;
 
   float* lutDec = reinterpret_cast<float*>(smem + kLutDecodeOff);
   float* lutThr = reinterpret_cast<float*>(smem + kLutThrOff);
@@ -470,18 +561,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     lutDec[code * 64 + 32 + l] = __uint_as_float(c_alphaDecodeBits[code]);
     if (code < kThrRows) lutThr[code * 32 + l] = __uint_as_float(c_srgbThresholdBits[code]);
   }
-  GroupCtx G;
-  G.tiles = reinterpret_cast<const uint32_t*>(smem + kStageOff + g * kStages * kTileBytes);
-  G.stage0 = smemAddr(G.tiles);
-  G.bar0 = smemAddr(smem + kBarOff + g * kStages * 8);
-  G.relCnt = reinterpret_cast<uint32_t*>(smem + kCntOff) + 2 * g;
-  G.xchgCnt = G.relCnt + 1;
-  G.xchg = reinterpret_cast<float4*>(smem + kXchgOff) + g * kXchgRing * 16;
-  if (gtid == 0) {
-    for (uint32_t s = 0; s < kStages; ++s)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(G.bar0 + 8 * s) : "memory");
-    *G.relCnt = 0;
-    *G.xchgCnt = 0;
+  if (tid == 0) {
+    for (uint32_t g = 0; g < kGroups; ++g) {
+      const GroupCtx G = groupCtx(g);
+      for (uint32_t s = 0; s < kStages; ++s) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(G.full0 + 8 * s) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(G.empty0 + 8 * s), "r"(kGroupWarps) : "memory");
+      }
+      for (uint32_t b = 0; b < kXchgRing; ++b) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(G.xfull0 + 8 * b), "r"(kGroupWarps) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(G.xempty0 + 8 * b) : "memory");
+      }
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -490,24 +581,27 @@ __global__ void __launch_bounds__(kThreads, 1)
   const FusedStage& s0 = p.st[0];
   const uint32_t regions = s0.regionsX * s0.regionsY;
   const uint32_t groupsTotal = gridDim.x * kGroups;
-  const uint32_t gid = g * gridDim.x + blockIdx.x;
-  if (gtid == 0) {
+  if (warp >= kProducerWarp0 && lane == 0) {  // the first two regions of the group
+    const uint32_t g = warp - kProducerWarp0;
+    const GroupCtx G = groupCtx(g);
     for (uint32_t s = 0; s < kStages; ++s) {
-      const uint32_t r = gid + s * groupsTotal;
+      const uint32_t r = g * gridDim.x + blockIdx.x + s * groupsTotal;
       if (r < regions)
         tmaLoadRegion(G.stage0 + s * kTileBytes, &tmap, (r % s0.regionsX) * kTile, (r / s0.regionsX) * kTile,
-                      G.bar0 + 8 * s);
+                      G.full0 + 8 * s);
     }
   }
-  const bool ok = mainLoopN(s0, &tmap, G, gid, groupsTotal, wig, lane, L);
+  __syncwarp();
+  const bool ok = mainLoopN(s0, &tmap, warp, groupsTotal, lane, L);
   if (!ok && lane == 0) {
-    // A load never completed: record it and give every in-flight load of
-    // this group one more bounded wait before the CTA may exit.
+    // A bounded wait gave up: record it and give the loads that may still be
+    // in flight one more bounded wait before the CTA may exit.
     atomicExch(p.errorFlag, 1u);
-    for (uint32_t s = 0; s < kStages; ++s) {
-      mbarWait(G.bar0 + 8 * s, 0);
-      mbarWait(G.bar0 + 8 * s, 1);
-    }
+    for (uint32_t g = 0; g < kGroups; ++g)
+      for (uint32_t s = 0; s < kStages; ++s) {
+        mbarWait(groupCtx(g).full0 + 8 * s, 0);
+        mbarWait(groupCtx(g).full0 + 8 * s, 1);
+      }
   }
   if (__syncthreads_or(!ok) || p.stageCount < 2) return;
 
@@ -521,8 +615,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       __threadfence();
     }
   }
-  if (!__syncthreads_or(last)) return;
-  uint32_t* tile = reinterpret_cast<uint32_t*>(smem + kStageOff + g * kStages * kTileBytes);
+  if (!__syncthreads_or(last) || warp >= kProducerWarp0) return;
+  const uint32_t g = warp / kGroupWarps, wig = warp % kGroupWarps, gtid = tid % kGroupThreads;
+  const GroupCtx G = groupCtx(g);
+  uint32_t* tile = const_cast<uint32_t*>(G.tiles);
   for (uint32_t d = 1; d < p.stageCount; ++d) {
     const FusedStage& st = p.st[d];
     const uint32_t nreg = st.regionsX * st.regionsY;
@@ -533,7 +629,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       tailRegionN(st, x0, y0, tile, G.xchg + (it % kXchgRing) * 16, g, wig, lane, it, L);
       groupSync(g);
     }
-    __syncthreads();
+    // consumer warps only (the producer warps have left)
+    asm volatile("bar.sync 5, %0;" ::"r"(kConsumerThreads) : "memory");
   }
 }
 
@@ -551,7 +648,14 @@ __global__ void debugEncodeKernel(const float* x, uint8_t* fast, uint8_t* exact,
     const float v = x[i];
     // The fast encoder's table index is derived from the value; keep it in
     // the encoder's domain [0, 1] (NaN -> 0) whatever the caller passes.
-    fast[i] = uint8_t(encodeChannel(fminf(fmaxf(v, 0.0f), 1.0f), L));
+    // The value goes through the packed texel encoder in channel i % 3, with
+    // its neighbours in the array as the other channels.
+    auto dom = [](float f) { return fminf(fmaxf(f, 0.0f), 1.0f); };
+    const float u = dom(x[(i + 1) % n]), w = dom(x[(i + 2) % n]), cv = dom(v);
+    const uint32_t ch = uint32_t(i % 3);
+    const float4 t = ch == 0 ? make_float4(cv, u, w, 0.5f) : ch == 1 ? make_float4(u, cv, w, 0.5f)
+                                                                    : make_float4(u, w, cv, 0.5f);
+    fast[i] = uint8_t(encodeTexel(t, L) >> (8 * ch));
     uint32_t c = 0;  // the oracle's threshold count (binary search)
     for (uint32_t step = 128; step > 0; step >>= 1)
       if (c + step <= 255 && full[c + step - 1] <= v) c += step;
