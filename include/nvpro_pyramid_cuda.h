@@ -267,6 +267,30 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerate(
     NvproPyramidCmd cmd, NvproPyramidStream stream, NvproPyramidPipelines pipelines,
     const NvproPyramidImage* pImage, uint32_t mipLevels);
 
+/* The whole default chain (both pipelines of `preset`, mipLevels == 0 for the
+ * full chain) on `stream`, without allocating anything.  No counterpart in the
+ * reference.
+ *
+ * For callers that cannot allocate device memory: code running where a host
+ * application owns every device allocation (plugins, fixed memory budgets),
+ * and hot loops that must not call cudaMalloc/cudaFree (cudaFree synchronises
+ * the device).  nvproPyramidCreateCmd allocates a few bytes of device counters;
+ * this entry point instead uses a fixed 256-byte __device__ array of the
+ * library (64 words, two per TMA launch of the chain: more than any chain
+ * needs; a chain that needed more would be rejected with
+ * NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT).  Every GPU that loads the library
+ * holds the array until the process exits.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the array and it keeps the last
+ * call's contents; each call clears it on `stream` first.  Calls whose work
+ * overlaps on the GPU (e.g. on two streams without ordering) race on it:
+ * order them. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerateNoAlloc(
+    NvproPyramidStream stream, NvproPyramidPreset preset, const NvproPyramidImage* pImage,
+    uint32_t mipLevels);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

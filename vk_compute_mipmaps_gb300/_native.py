@@ -111,6 +111,7 @@ SIGNATURES = {
                                                         POINTER(NvproPyramidState)]),
     "nvproPyramidCmdDeviceStatus": (c_int, [c_void_p]),
     "nvproPyramidDebugSrgbEncode": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
+    "nvproPyramidGenerateNoAlloc": (c_int, [c_void_p, c_int, POINTER(NvproPyramidImage), c_uint32]),
     "nvproPyramidGenerate": (c_int, [c_void_p, c_void_p, NvproPyramidPipelines, POINTER(NvproPyramidImage),
                                      c_uint32]),
 }

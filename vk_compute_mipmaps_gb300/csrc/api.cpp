@@ -545,6 +545,90 @@ NvproPyramidResult nvproPyramidDebugSrgbEncode(NvproPyramidStream stream, const 
   return NVPRO_PYRAMID_SUCCESS;
 }
 
+NvproPyramidResult nvproPyramidGenerateNoAlloc(NvproPyramidStream stream, NvproPyramidPreset preset,
+                                               const NvproPyramidImage* pImage, uint32_t mipLevels) {
+  // The default schedule (nvpro_pyramid_dispatch.hpp:109-304 with both
+  // pipelines) is built in fixed-size stack arrays: no command object, no
+  // device or host allocation on the way to the launches.
+  if (!pImage) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pImage is NULL");
+  if (presetBytes(uint32_t(preset)) == 0)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "unknown preset %d", int(preset));
+  const uint32_t w = pImage->width, h = pImage->height;
+  if (w == 0 || h == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "zero width or height");
+  const uint32_t full = nvproPyramidFullLevelCount(w, h);
+  if (mipLevels == 0) mipLevels = full;
+  if (mipLevels > full || mipLevels > NVPRO_PYRAMID_MAX_LEVELS || pImage->levelCount < mipLevels)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u levels requested; %ux%u image binds %u of at most %u",
+                mipLevels, w, h, pImage->levelCount, full);
+  Record rec;
+  std::memset(&rec, 0, sizeof rec);
+  rec.image = *pImage;
+  rec.info.preset = uint32_t(preset);
+  rec.info.groupCountY = rec.info.groupCountZ = 1;
+  DispatchParams params[NVPRO_PYRAMID_MAX_LEVELS];
+  uint32_t count = 0;
+  NvproPyramidState st{0u, mipLevels - 1u, w, h};
+  while (st.remainingLevels != 0) {
+    uint32_t done = 0, groups = 0;
+    bool fast = false;
+    if (st.currentX % 4 == 0 && st.currentY % 4 == 0) {  // nvproPyramidDefaultFastDispatcher<4, 6>
+      uint32_t x = st.currentX, y = st.currentY;
+      while (x % 2 == 0 && y % 2 == 0 && done < st.remainingLevels && done < 6) {
+        x /= 2;
+        y /= 2;
+        ++done;
+      }
+      fast = true;
+      const uint32_t shift = done > 5 ? 12u : 10u, mask = done > 5 ? 4095u : 1023u;
+      groups = (st.currentX * st.currentY + mask) >> shift;
+    } else {  // nvproPyramidDefaultGeneralDispatcher
+      done = st.remainingLevels >= 2 ? 2u : st.remainingLevels;
+      const uint32_t dw = std::max(st.currentX >> done, 1u), dh = std::max(st.currentY >> done, 1u);
+      groups = done == 1 ? (dw * dh + 127) / 128 : ((dw + 7) / 8) * ((dh + 7) / 8);
+    }
+    rec.info.isFastPipeline = fast;
+    rec.info.pushConstant = st.currentLevel << NVPRO_PYRAMID_INPUT_LEVEL_SHIFT | done;
+    rec.info.groupCountX = groups;
+    NvproPyramidResult r = makeParams(rec, &params[count]);
+    if (r != NVPRO_PYRAMID_SUCCESS) return r;
+    ++count;
+    st.currentLevel += done;
+    st.remainingLevels -= done;
+    st.currentX = std::max(st.currentX >> done, 1u);
+    st.currentY = std::max(st.currentY >> done, 1u);
+  }
+  if (count == 0) return NVPRO_PYRAMID_SUCCESS;
+
+  uint32_t* scratch = nullptr;
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  cudaError_t e = staticScratch(&scratch);
+  // Calls share the array and it keeps the last call's contents: start from zero.
+  if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, kStaticScratchWords * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "static scratch: %s", cudaGetErrorString(e));
+  uint32_t launches = 0, tmaLaunches = 0;
+  uint32_t i = 0;
+  while (i < count) {
+    const DispatchParams& p = params[i];
+    if (p.isFast && tmaFastSupported(p)) {
+      uint32_t j = i + 1;
+      while (j < count && j - i < tmaMaxFused() && tmaTailCompatible(params[j - 1], params[j])) ++j;
+      if (2 * (tmaLaunches + 1) > kStaticScratchWords)
+        return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT,
+                    "chain needs %u scratch words; the fixed scratch holds %u", 2 * (tmaLaunches + 1),
+                    kStaticScratchWords);
+      const Scratch sc{scratch + 2 * tmaLaunches, 2};
+      e = launchTmaFast(p, j > i + 1 ? &params[i + 1] : nullptr, j - i - 1, s, sc, &launches);
+      ++tmaLaunches;
+      i = j;
+    } else {
+      e = launchPortable(p, s, &launches);
+      ++i;
+    }
+    if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  }
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
 NvproPyramidResult nvproPyramidGenerate(NvproPyramidCmd cmd, NvproPyramidStream stream,
                                         NvproPyramidPipelines pipelines, const NvproPyramidImage* pImage,
                                         uint32_t mipLevels) {

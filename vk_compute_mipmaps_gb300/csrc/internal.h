@@ -56,4 +56,11 @@ cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uin
 constexpr uint32_t kCounterLastCta = 0;
 constexpr uint32_t kCounterError = 1;
 
+// The fixed device scratch of nvproPyramidGenerateNoAlloc: kStaticScratchWords
+// words in a file-scope __device__ array.  Returns its device address for the
+// current device, doing the per-device look-up (cudaGetSymbolAddress) on first
+// use.
+constexpr uint32_t kStaticScratchWords = 64;
+cudaError_t staticScratch(uint32_t** ptr);
+
 }  // namespace nvpyr

@@ -791,6 +791,32 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
   return cudaGetLastError();
 }
 
+// Device scratch for nvproPyramidGenerateNoAlloc: the last-CTA counter and
+// the wait-error flag of each TMA launch of a chain, two words per launch.
+// It is a file-scope __device__ array, so every GPU that loads the library
+// holds these 256 bytes until the process exits, and no call allocates.
+static __device__ __align__(256) uint32_t g_staticScratch[kStaticScratchWords];
+
+cudaError_t staticScratch(uint32_t** ptr) {
+  static uint32_t* addrs[64] = {};
+  static std::mutex mu;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addrs[dev]) {
+    // In host code the array's name is a host-side stand-in; its device
+    // address comes from the runtime, once per device, with that device current.
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_staticScratch);
+    if (e != cudaSuccess) return e;
+    addrs[dev] = static_cast<uint32_t*>(p);
+  }
+  *ptr = addrs[dev];
+  return cudaSuccess;
+}
+
 cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, cudaStream_t stream) {
   DeviceInfo* info = nullptr;
   cudaError_t e = deviceInfo(&info);
