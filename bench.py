@@ -197,6 +197,43 @@ def bench_config(w, h, dev, stream, flush, steps):
     return out
 
 
+def bench_float_adjoint(dev, stream, flush, steps):
+    """Linear float pyramids: forward (levels 1..) and adjoint (base gradient
+    from upstream gradients of levels 1..) through the torch.autograd.Function
+    helpers.  Algorithmic bytes: forward = base read + levels written;
+    adjoint = upstream gradients read + base gradient written."""
+    import torch
+    from vk_compute_mipmaps_gb300 import autograd as A
+    from vk_compute_mipmaps_gb300.pyramid import level_sizes
+    peak, _ = measured_peak()
+    out = {}
+    for name, B, S, dt in (("fp32_8x2048x2048", 8, 2048, torch.float32),
+                           ("fp32_16384x16384", 1, 16384, torch.float32),
+                           ("fp16_16384x16384", 1, 16384, torch.float16)):
+        g = torch.Generator(device=dev).manual_seed(11)
+        base = torch.rand((B, S, S, 4), generator=g, device=dev).to(dt)
+        sizes = level_sizes(S, S)
+        ups = [None] + [torch.randn((B, h, w, 4), generator=g, device=dev).to(dt) for w, h in sizes[1:]]
+        esz = base.element_size() * 4
+        base_bytes = B * S * S * esz
+        lvl_bytes = B * sum(w * h for w, h in sizes[1:]) * esz
+        with torch.cuda.stream(stream):
+            fwd = time_loop(lambda: A.forward_levels(base), stream, steps, 3, flush=flush)
+            bwd = time_loop(lambda: A.adjoint(ups, tuple(base.shape), dt, dev), stream, steps, 3, flush=flush)
+            both = time_loop(lambda: (A.forward_levels(base), A.adjoint(ups, tuple(base.shape), dt, dev)),
+                             stream, steps, 3, flush=flush)
+        f_us, b_us, fb_us = (statistics.median(t) * 1e3 for t in (fwd, bwd, both))
+        fb = base_bytes + lvl_bytes
+        out[name] = {"forward_us": round(f_us, 2), "adjoint_us": round(b_us, 2), "fwd_plus_bwd_us": round(fb_us, 2),
+                     "fwd_plus_bwd_over_fwd": round(fb_us / f_us, 3),
+                     "forward_frac_of_hbm_peak": round(fb / (f_us * 1e-6) / 1e9 / peak, 4),
+                     "adjoint_frac_of_hbm_peak": round(fb / (b_us * 1e-6) / 1e9 / peak, 4),
+                     "algorithmic_bytes_each": fb}
+        del base, ups
+        torch.cuda.empty_cache()
+    return out
+
+
 def cpu_baseline_sample(threads: int, reps: int = 1):
     """The restated reference CPU generator on `threads` host threads, one
     4096^2 image per thread (as the reference benchmark runs one image per
@@ -304,6 +341,7 @@ def run_ours(args, rank, world):
             torch.cuda.empty_cache()
             for cw, ch in CONFIGS:
                 extra[f"{cw}x{ch}"] = bench_config(cw, ch, dev, stream, flush, max(10, min(args.steps, 100)))
+            extra["float_adjoint"] = bench_float_adjoint(dev, stream, flush, max(5, min(args.steps, 20)))
             del flush
         if not args.no_cpu:
             threads = os.cpu_count() or 1

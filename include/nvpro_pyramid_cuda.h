@@ -267,6 +267,30 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerate(
     NvproPyramidCmd cmd, NvproPyramidStream stream, NvproPyramidPipelines pipelines,
     const NvproPyramidImage* pImage, uint32_t mipLevels);
 
+/* ------------------------------------------------------------------------ */
+/* Adjoint of the linear float pyramids.  No reference counterpart (the      */
+/* reference template admits float types, nvpro_pyramid.glsl:44-46, but has  */
+/* no gradient).                                                             */
+/* ------------------------------------------------------------------------ */
+
+/* Bytes of FP32 workspace nvproPyramidAdjoint needs for a w x h chain of
+ * mipLevels levels (0 = full chain): the intermediate levels of the sweep. */
+NVPRO_PYRAMID_API uint64_t nvproPyramidAdjointWorkspaceBytes(uint32_t width, uint32_t height,
+                                                             uint32_t mipLevels);
+
+/* Gradient of sum_k <upstream_k, level_k> with respect to the base level, for
+ * the RGBA32F or RGBA16F preset (FP32 arithmetic).  `upstream` holds the
+ * upstream gradient of every level in the preset's storage type
+ * (upstream->levels[k] may be NULL: zero gradient); the result is written to
+ * baseGrad (preset storage type, row pitch baseGradPitch or tightly packed if
+ * 0).  The sweep follows the forward's default dispatch schedule coarse to
+ * fine; each texel of baseGrad is written once.  workspace: device memory of
+ * nvproPyramidAdjointWorkspaceBytes bytes, 16-byte aligned. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidAdjoint(
+    NvproPyramidStream stream, NvproPyramidPreset preset, const NvproPyramidImage* upstream,
+    void* baseGrad, uint64_t baseGradPitch, uint32_t mipLevels, void* workspace,
+    uint64_t workspaceBytes);
+
 /* The whole default chain (both pipelines of `preset`, mipLevels == 0 for the
  * full chain) on `stream`, without allocating anything.  No counterpart in the
  * reference.

@@ -545,6 +545,186 @@ NvproPyramidResult nvproPyramidDebugSrgbEncode(NvproPyramidStream stream, const 
   return NVPRO_PYRAMID_SUCCESS;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The default dispatch schedule (nvpro_pyramid_dispatch.hpp:109-304 with a
+// fast pipeline): isFast, input level and level count of each dispatch.
+struct SchedEntry {
+  uint32_t isFast, level, count, groups;
+};
+
+uint32_t defaultSchedule(uint32_t w, uint32_t h, uint32_t mipLevels, SchedEntry* out) {
+  uint32_t n = 0;
+  NvproPyramidState st{0u, mipLevels - 1u, w, h};
+  while (st.remainingLevels != 0) {
+    uint32_t done = 0, groups = 0, fast = 0;
+    if (st.currentX % 4 == 0 && st.currentY % 4 == 0) {  // nvproPyramidDefaultFastDispatcher<4, 6>
+      uint32_t x = st.currentX, y = st.currentY;
+      while (x % 2 == 0 && y % 2 == 0 && done < st.remainingLevels && done < 6) {
+        x /= 2;
+        y /= 2;
+        ++done;
+      }
+      fast = 1;
+      const uint32_t shift = done > 5 ? 12u : 10u, mask = done > 5 ? 4095u : 1023u;
+      groups = (st.currentX * st.currentY + mask) >> shift;
+    } else {  // nvproPyramidDefaultGeneralDispatcher
+      done = st.remainingLevels >= 2 ? 2u : st.remainingLevels;
+      const uint32_t dw = std::max(st.currentX >> done, 1u), dh = std::max(st.currentY >> done, 1u);
+      groups = done == 1 ? (dw * dh + 127) / 128 : ((dw + 7) / 8) * ((dh + 7) / 8);
+    }
+    out[n++] = SchedEntry{fast, st.currentLevel, done, groups};
+    st.currentLevel += done;
+    st.remainingLevels -= done;
+    st.currentX = std::max(st.currentX >> done, 1u);
+    st.currentY = std::max(st.currentY >> done, 1u);
+  }
+  return n;
+}
+
+// Levels whose adjoint values the sweep materialises in the workspace (all
+// input levels of dispatches except 0, and the middle level of 2-level
+// general dispatches), with their byte offsets.
+uint64_t adjointWorkspaceLayout(uint32_t w, uint32_t h, uint32_t mipLevels, uint64_t* offsets) {
+  SchedEntry sched[NVPRO_PYRAMID_MAX_LEVELS];
+  const uint32_t n = defaultSchedule(w, h, mipLevels, sched);
+  bool need[NVPRO_PYRAMID_MAX_LEVELS] = {};
+  for (uint32_t i = 0; i < n; ++i) {
+    if (sched[i].level > 0) need[sched[i].level] = true;
+    if (!sched[i].isFast && sched[i].count == 2) need[sched[i].level + 1] = true;
+  }
+  uint64_t off = 0;
+  for (uint32_t k = 0; k < mipLevels; ++k) {
+    offsets[k] = need[k] ? off : UINT64_MAX;
+    if (need[k]) off += uint64_t(levelDim(w, k)) * levelDim(h, k) * 16;
+  }
+  return off;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t nvproPyramidAdjointWorkspaceBytes(uint32_t width, uint32_t height, uint32_t mipLevels) {
+  const uint32_t full = nvproPyramidFullLevelCount(width, height);
+  if (width == 0 || height == 0) return 0;
+  if (mipLevels == 0) mipLevels = full;
+  if (mipLevels > full) return 0;
+  uint64_t offsets[NVPRO_PYRAMID_MAX_LEVELS];
+  return adjointWorkspaceLayout(width, height, mipLevels, offsets);
+}
+
+NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPreset preset,
+                                       const NvproPyramidImage* upstream, void* baseGrad, uint64_t baseGradPitch,
+                                       uint32_t mipLevels, void* workspace, uint64_t workspaceBytes) {
+  if (preset != NVPRO_PYRAMID_PRESET_RGBA32F && preset != NVPRO_PYRAMID_PRESET_RGBA16F)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "the adjoint exists for the linear float presets only");
+  if (!upstream || !baseGrad) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "NULL upstream or baseGrad");
+  const uint32_t w = upstream->width, h = upstream->height;
+  const uint32_t full = nvproPyramidFullLevelCount(w, h);
+  if (w == 0 || h == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "zero width or height");
+  if (mipLevels == 0) mipLevels = full;
+  if (mipLevels > full || upstream->levelCount < mipLevels)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u levels requested; upstream binds %u of at most %u",
+                mipLevels, upstream->levelCount, full);
+  const uint32_t bpp = presetBytes(uint32_t(preset));
+  const uint32_t gType = preset == NVPRO_PYRAMID_PRESET_RGBA32F ? 0u : 1u;
+  if (baseGradPitch == 0) baseGradPitch = uint64_t(w) * bpp;
+  if (baseGradPitch < uint64_t(w) * bpp || baseGradPitch % bpp || reinterpret_cast<uintptr_t>(baseGrad) % bpp)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "baseGrad pitch/alignment invalid");
+  for (uint32_t k = 0; k < mipLevels; ++k) {
+    const uint64_t pitch = upstream->rowPitchBytes[k] ? upstream->rowPitchBytes[k] : uint64_t(levelDim(w, k)) * bpp;
+    if (upstream->levels[k] &&
+        (reinterpret_cast<uintptr_t>(upstream->levels[k]) % bpp || pitch % bpp || pitch < uint64_t(levelDim(w, k)) * bpp))
+      return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "upstream level %u pitch/alignment invalid", k);
+  }
+  uint64_t wsOff[NVPRO_PYRAMID_MAX_LEVELS];
+  const uint64_t wsNeed = adjointWorkspaceLayout(w, h, mipLevels, wsOff);
+  if (wsNeed > workspaceBytes || (wsNeed && (!workspace || reinterpret_cast<uintptr_t>(workspace) % 16)))
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "workspace of %llu bytes (16-byte aligned) needed, got %llu",
+                (unsigned long long)wsNeed, (unsigned long long)workspaceBytes);
+  if (mipLevels == 1) {  // no levels above the base: the gradient is the upstream one
+    const uint64_t rowBytes = uint64_t(w) * bpp;
+    const uint64_t srcPitch = upstream->rowPitchBytes[0] ? upstream->rowPitchBytes[0] : rowBytes;
+    cudaError_t e = upstream->levels[0]
+                        ? cudaMemcpy2DAsync(baseGrad, baseGradPitch, upstream->levels[0], srcPitch, rowBytes, h,
+                                            cudaMemcpyDeviceToDevice, reinterpret_cast<cudaStream_t>(stream))
+                        : cudaMemset2DAsync(baseGrad, baseGradPitch, 0, rowBytes, h,
+                                            reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? NVPRO_PYRAMID_SUCCESS : fail(NVPRO_PYRAMID_ERROR_CUDA, "%s", cudaGetErrorString(e));
+  }
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  uint8_t* ws = static_cast<uint8_t*>(workspace);
+  // Where h_k lives: level 0 -> baseGrad; materialised levels -> workspace;
+  // the top level -> the upstream gradient itself.
+  auto hPtr = [&](uint32_t k) { return k == 0 ? static_cast<uint8_t*>(baseGrad) : ws + wsOff[k]; };
+  auto hPitch = [&](uint32_t k) { return k == 0 ? baseGradPitch : uint64_t(levelDim(w, k)) * 16; };
+  auto hType = [&](uint32_t k) { return k == 0 ? gType : 0u; };
+  auto gPtr = [&](uint32_t k) { return static_cast<const uint8_t*>(upstream->levels[k]); };
+  auto gPitch = [&](uint32_t k) {
+    return upstream->rowPitchBytes[k] ? upstream->rowPitchBytes[k] : uint64_t(levelDim(w, k)) * bpp;
+  };
+  SchedEntry sched[NVPRO_PYRAMID_MAX_LEVELS];
+  const uint32_t n = defaultSchedule(w, h, mipLevels, sched);
+  const uint32_t top = mipLevels - 1;
+  for (int i = int(n) - 1; i >= 0; --i) {
+    const SchedEntry& d = sched[i];
+    const uint32_t L = d.level, hi = d.level + d.count;
+    // h of level `hi`: the upstream gradient if it is the top level
+    const uint8_t* srcTop = hi == top ? gPtr(top) : hPtr(hi);
+    const uint64_t srcPitch = hi == top ? gPitch(top) : hPitch(hi);
+    const uint32_t srcType = hi == top ? gType : 0u;
+    cudaError_t e;
+    if (d.isFast) {
+      AdjointChainParams p{};
+      p.n = d.count;
+      p.w = levelDim(w, L);
+      p.h = levelDim(h, L);
+      p.gType = gType;
+      for (uint32_t k = 0; k < d.count; ++k) {
+        p.g[k] = gPtr(L + k);
+        p.gPitch[k] = gPitch(L + k);
+      }
+      p.top = srcTop;
+      p.topPitch = srcPitch;
+      p.topType = srcType;
+      p.out = hPtr(L);
+      p.outPitch = hPitch(L);
+      p.outType = hType(L);
+      e = launchAdjointChain(p, s);
+    } else {
+      e = cudaSuccess;
+      const uint8_t* hc = srcTop;
+      uint64_t hcPitch = srcPitch;
+      uint32_t hcType = srcType;
+      for (int k = int(hi) - 1; k >= int(L) && e == cudaSuccess; --k) {
+        AdjointLevelParams p{};
+        p.fw = levelDim(w, k);
+        p.fh = levelDim(h, k);
+        p.cw = levelDim(w, k + 1);
+        p.ch = levelDim(h, k + 1);
+        p.g = gPtr(k);
+        p.gPitch = gPitch(k);
+        p.gType = gType;
+        p.hc = hc;
+        p.hcPitch = hcPitch;
+        p.hcType = hcType;
+        p.out = hPtr(k);
+        p.outPitch = hPitch(k);
+        p.outType = hType(k);
+        e = launchAdjointLevel(p, s);
+        hc = hPtr(k);
+        hcPitch = hPitch(k);
+        hcType = hType(k);
+      }
+    }
+    if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "adjoint launch failed: %s", cudaGetErrorString(e));
+  }
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
 NvproPyramidResult nvproPyramidGenerateNoAlloc(NvproPyramidStream stream, NvproPyramidPreset preset,
                                                const NvproPyramidImage* pImage, uint32_t mipLevels) {
   // The default schedule (nvpro_pyramid_dispatch.hpp:109-304 with both

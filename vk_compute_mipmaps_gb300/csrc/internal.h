@@ -52,6 +52,36 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
 // Test support: the fast sRGB encoder and the exact threshold count, per float.
 cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, cudaStream_t stream);
 
+// Adjoint of the linear float pyramids (kernels_adjoint.cu).  Gradient
+// levels are RGBA FP32 (type 0) or RGBA FP16 (type 1); a null level reads as 0.
+struct AdjointChainParams {
+  uint32_t n;  // levels of the fast dispatch
+  uint32_t w, h;  // size of level L
+  uint32_t gType;
+  const uint8_t* g[kMaxDispatchLevels];  // upstream gradient of levels L..L+n-1
+  uint64_t gPitch[kMaxDispatchLevels];
+  const uint8_t* top;  // h of level L+n
+  uint64_t topPitch;
+  uint32_t topType;
+  uint32_t outType;
+  uint8_t* out;  // h of level L
+  uint64_t outPitch;
+};
+struct AdjointLevelParams {
+  uint32_t fw, fh, cw, ch;  // fine level k, coarse level k+1
+  const uint8_t* g;         // upstream gradient of level k
+  uint64_t gPitch;
+  uint32_t gType;
+  const uint8_t* hc;  // h of level k+1
+  uint64_t hcPitch;
+  uint32_t hcType;
+  uint8_t* out;  // h of level k
+  uint64_t outPitch;
+  uint32_t outType;
+};
+cudaError_t launchAdjointChain(const AdjointChainParams& p, cudaStream_t stream);
+cudaError_t launchAdjointLevel(const AdjointLevelParams& p, cudaStream_t stream);
+
 // Scratch counter slots.
 constexpr uint32_t kCounterLastCta = 0;
 constexpr uint32_t kCounterError = 1;
