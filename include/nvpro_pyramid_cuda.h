@@ -205,6 +205,13 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugSrgbEncode(
     NvproPyramidStream stream, const float* x, uint8_t* fast, uint8_t* exact, uint64_t n);
 
+/* Test support (no reference counterpart): the alpha byte of the kernels'
+ * texel encoder for each float of x (clamped to [0, 1] first) into `fast`, and
+ * clamp(uint(a * 255 + 0.5), 0, 255) with separately rounded operations
+ * (srgba8_mipmap_preamble.glsl:125) into `exact`. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugAlphaEncode(
+    NvproPyramidStream stream, const float* x, uint8_t* fast, uint8_t* exact, uint64_t n);
+
 /* ------------------------------------------------------------------------ */
 /* The dispatcher (nvpro_pyramid_dispatch.hpp:54-304).                       */
 /* ------------------------------------------------------------------------ */
@@ -300,9 +307,9 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidAdjoint(
  * and hot loops that must not call cudaMalloc/cudaFree (cudaFree synchronises
  * the device).  nvproPyramidCreateCmd allocates a few bytes of device counters;
  * this entry point instead uses a fixed 256-byte __device__ array of the
- * library (64 words, two per TMA launch of the chain: more than any chain
- * needs; a chain that needed more would be rejected with
- * NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT).  Every GPU that loads the library
+ * library (64 words: two per TMA launch and four per run of general
+ * dispatches of the chain, more than any chain needs; a chain that needed
+ * more would be rejected with NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT).  Every GPU that loads the library
  * holds the array until the process exits.
  *
  * The first call on a device looks up the array's device address

@@ -90,6 +90,28 @@ def test_srgba8_bit_exact(cuda, w, h, flags):
     assert_same(got, oracle_bytes(N.PRESET_SRGBA8, base, sched, mips), w, h, 4, mips, f"{w}x{h} flags={flags}")
 
 
+# Every (w mod 4, h mod 4) but (0, 0) starts with a general dispatch whose
+# kernel sizes are (2|w&1, 2|h&1) on level 0 and (2|(w>>1)&1, ...) on level 1:
+# all fifteen two-level strip kernels, plus strips and bands that end mid-way.
+MOD4 = [(300 + a, 200 + b) for a in range(4) for b in range(4) if (a, b) != (0, 0)]
+
+
+@pytest.mark.parametrize("w,h", MOD4 + [(1001, 999), (2050, 1027), (4093, 45), (45, 4093), (6, 1023)])
+def test_general_strips_bit_exact(cuda, w, h):
+    base = random_base(N.PRESET_SRGBA8, w, h, w * 7 + h)
+    mips = P.full_level_count(w, h)
+    got, sched, _ = gpu_run(cuda, N.PRESET_SRGBA8, base)
+    assert_same(got, oracle_bytes(N.PRESET_SRGBA8, base, sched, mips), w, h, 4, mips, f"{w}x{h}")
+
+
+@pytest.mark.parametrize("w,h", [(1001, 999), (1000, 999), (1001, 998), (1002, 1002), (3, 700), (700, 3)])
+def test_general_one_level_bit_exact(cuda, w, h):
+    """mipLevels = 2: a single one-level general dispatch (the four one-level strip kernels)."""
+    base = random_base(N.PRESET_SRGBA8, w, h, w + 3 * h)
+    got, sched, _ = gpu_run(cuda, N.PRESET_SRGBA8, base, mips=2)
+    assert_same(got, oracle_bytes(N.PRESET_SRGBA8, base, sched, 2), w, h, 4, 2, f"{w}x{h} mips=2")
+
+
 @pytest.mark.parametrize("w,h", BIG)
 def test_srgba8_bit_exact_large(cuda, w, h):
     from test_oracle_pins import smooth_field
@@ -264,6 +286,39 @@ def test_fast_srgb_encoder_exhaustive(cuda, native):
     torch.cuda.synchronize()
     assert np.array_equal(exact.cpu().numpy(), O.srgb_encode_array(xs))
     assert np.array_equal(fast.cpu().numpy(), O.srgb_encode_array(xs))
+
+
+def test_fast_alpha_encoder_exhaustive(cuda, native):
+    """The texel encoder's alpha byte equals clamp(uint(rn(rn(a*255)+0.5))) for
+    every FP32 a in [0, 1]; the GPU's scalar reference equals the oracle's."""
+    import torch
+    lo, hi = 0, int(np.float32(1.0).view(np.uint32))
+    chunk = 1 << 28
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    for start in range(lo, hi + 1, chunk):
+        bits = torch.arange(start, min(start + chunk, hi + 1), dtype=torch.int64, device=cuda).to(torch.int32)
+        x = bits.view(torch.float32)
+        fast = torch.empty(x.numel(), dtype=torch.uint8, device=cuda)
+        exact = torch.empty_like(fast)
+        N.check(native.nvproPyramidDebugAlphaEncode(stream, x.data_ptr(), fast.data_ptr(), exact.data_ptr(),
+                                                    x.numel()))
+        torch.cuda.synchronize()
+        bad = (fast != exact).nonzero()
+        assert bad.numel() == 0, f"{bad.numel()} mismatches, first a={x[bad[0]].item()!r}"
+    # a*255+0.5 just below / at each integer, and random values: the oracle agrees
+    k = np.arange(256, dtype=np.float32)
+    edges = ((k + np.float32(0.5)) / np.float32(255)).astype(np.float32)
+    xs = np.concatenate([np.random.default_rng(2).random(1 << 14, dtype=np.float32),
+                         np.nextafter(edges, 0, dtype=np.float32), edges, np.nextafter(edges, 2, dtype=np.float32)])
+    xs = np.clip(xs, 0, 1).astype(np.float32)
+    xt = torch.from_numpy(xs).to(cuda)
+    fast = torch.empty(xs.size, dtype=torch.uint8, device=cuda)
+    exact = torch.empty_like(fast)
+    N.check(native.nvproPyramidDebugAlphaEncode(stream, xt.data_ptr(), fast.data_ptr(), exact.data_ptr(), xs.size))
+    torch.cuda.synchronize()
+    want = np.array([O.orc().orc_alpha_encode(float(v)) for v in xs], np.uint8)
+    assert np.array_equal(exact.cpu().numpy(), want)
+    assert np.array_equal(fast.cpu().numpy(), want)
 
 
 def test_no_device_wait_gave_up(cuda, native):

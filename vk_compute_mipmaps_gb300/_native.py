@@ -111,6 +111,7 @@ SIGNATURES = {
                                                         POINTER(NvproPyramidState)]),
     "nvproPyramidCmdDeviceStatus": (c_int, [c_void_p]),
     "nvproPyramidDebugSrgbEncode": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
+    "nvproPyramidDebugAlphaEncode": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
     "nvproPyramidAdjointWorkspaceBytes": (c_uint64, [c_uint32, c_uint32, c_uint32]),
     "nvproPyramidAdjoint": (c_int, [c_void_p, c_int, POINTER(NvproPyramidImage), c_void_p, c_uint64, c_uint32,
                                     c_void_p, c_uint64]),

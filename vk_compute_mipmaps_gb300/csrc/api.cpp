@@ -390,6 +390,12 @@ NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
       e = launchTmaFast(p, tail ? &params[i + 1] : nullptr, uint32_t(tail), cmd->stream, cmd->scratch,
                         &cmd->launches);
       i += 1 + tail;
+    } else if (!portableOnly && generalFastSupported(p)) {
+      // A run of general dispatches is one launch (fused unless NO_FUSION).
+      size_t j = i + 1;
+      while (fuse && j < params.size() && j - i < generalMaxStages() && generalFastSupported(params[j])) ++j;
+      e = launchGeneralChain(&params[i], uint32_t(j - i), cmd->stream, cmd->scratch, &cmd->launches);
+      i = j;
     } else {
       e = launchPortable(p, cmd->stream, &cmd->launches);
       i += 1;
@@ -540,7 +546,15 @@ NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd cmd) {
 NvproPyramidResult nvproPyramidDebugSrgbEncode(NvproPyramidStream stream, const float* x, uint8_t* fast,
                                                uint8_t* exact, uint64_t n) {
   if (!x || !fast || !exact) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "NULL buffer");
-  cudaError_t e = launchDebugEncode(x, fast, exact, n, reinterpret_cast<cudaStream_t>(stream));
+  cudaError_t e = launchDebugEncode(x, fast, exact, n, 0, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "debug encode: %s", cudaGetErrorString(e));
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidDebugAlphaEncode(NvproPyramidStream stream, const float* x, uint8_t* fast,
+                                                uint8_t* exact, uint64_t n) {
+  if (!x || !fast || !exact) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "NULL buffer");
+  cudaError_t e = launchDebugEncode(x, fast, exact, n, 1, reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "debug encode: %s", cudaGetErrorString(e));
   return NVPRO_PYRAMID_SUCCESS;
 }
@@ -785,20 +799,30 @@ NvproPyramidResult nvproPyramidGenerateNoAlloc(NvproPyramidStream stream, NvproP
   // Calls share the array and it keeps the last call's contents: start from zero.
   if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, kStaticScratchWords * sizeof(uint32_t), s);
   if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "static scratch: %s", cudaGetErrorString(e));
-  uint32_t launches = 0, tmaLaunches = 0;
+  // Each launch that needs scratch gets its own words of the fixed array:
+  // 2 per TMA launch (last-CTA counter, error flag), 4 per general chain.
+  uint32_t launches = 0, used = 0;
   uint32_t i = 0;
   while (i < count) {
     const DispatchParams& p = params[i];
     if (p.isFast && tmaFastSupported(p)) {
       uint32_t j = i + 1;
       while (j < count && j - i < tmaMaxFused() && tmaTailCompatible(params[j - 1], params[j])) ++j;
-      if (2 * (tmaLaunches + 1) > kStaticScratchWords)
-        return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT,
-                    "chain needs %u scratch words; the fixed scratch holds %u", 2 * (tmaLaunches + 1),
+      if (used + 2 > kStaticScratchWords)
+        return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "chain needs more than the %u fixed scratch words",
                     kStaticScratchWords);
-      const Scratch sc{scratch + 2 * tmaLaunches, 2};
+      const Scratch sc{scratch + used, 2};
       e = launchTmaFast(p, j > i + 1 ? &params[i + 1] : nullptr, j - i - 1, s, sc, &launches);
-      ++tmaLaunches;
+      used += 2;
+      i = j;
+    } else if (generalFastSupported(p)) {
+      uint32_t j = i + 1;
+      while (j < count && j - i < generalMaxStages() && generalFastSupported(params[j])) ++j;
+      if (used + kCounterBarrierGen + 1 > kStaticScratchWords)
+        return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "chain needs more than the %u fixed scratch words",
+                    kStaticScratchWords);
+      e = launchGeneralChain(&params[i], j - i, s, Scratch{scratch + used, kCounterBarrierGen + 1}, &launches);
+      used += kCounterBarrierGen + 1;
       i = j;
     } else {
       e = launchPortable(p, s, &launches);

@@ -50,7 +50,8 @@ uint32_t tmaMaxFused();
 cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, uint32_t tailCount,
                           cudaStream_t stream, const Scratch& scratch, uint32_t* launches);
 // Test support: the fast sRGB encoder and the exact threshold count, per float.
-cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, cudaStream_t stream);
+cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, uint32_t alpha,
+                              cudaStream_t stream);
 
 // Adjoint of the linear float pyramids (kernels_adjoint.cu).  Gradient
 // levels are RGBA FP32 (type 0) or RGBA FP16 (type 1); a null level reads as 0.
@@ -79,12 +80,25 @@ struct AdjointLevelParams {
   uint64_t outPitch;
   uint32_t outType;
 };
+// The general pipeline for sRGBA8 as streaming column strips
+// (kernels_general.cu): dispatches of 1 or 2 levels whose input level is at
+// least 2x2 (and level L+1 too, for 2 levels) with full workgroup coverage.
+// A run of up to generalMaxStages() such dispatches is one cooperative launch
+// with grid barriers between them; for more than one dispatch it uses scratch
+// words kCounterError, kCounterBarrier and kCounterBarrierGen.
+bool generalFastSupported(const DispatchParams& p);
+uint32_t generalMaxStages();
+cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStream_t stream, const Scratch& scratch,
+                               uint32_t* launches);
+
 cudaError_t launchAdjointChain(const AdjointChainParams& p, cudaStream_t stream);
 cudaError_t launchAdjointLevel(const AdjointLevelParams& p, cudaStream_t stream);
 
 // Scratch counter slots.
 constexpr uint32_t kCounterLastCta = 0;
 constexpr uint32_t kCounterError = 1;
+constexpr uint32_t kCounterBarrier = 2;     // general chain: CTAs arrived at the barrier
+constexpr uint32_t kCounterBarrierGen = 3;  // general chain: barrier generation
 
 // The fixed device scratch of nvproPyramidGenerateNoAlloc: kStaticScratchWords
 // words in a file-scope __device__ array.  Returns its device address for the

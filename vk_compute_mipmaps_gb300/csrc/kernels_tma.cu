@@ -44,7 +44,7 @@
 #include <atomic>
 #include <mutex>
 
-#include "device_common.cuh"
+#include "srgb_codec.cuh"
 
 namespace nvpyr {
 namespace {
@@ -68,7 +68,6 @@ constexpr uint32_t kWaitBackoffNs = 128;
 
 // Byte offsets inside the dynamic shared memory block.
 constexpr uint32_t kLutDecodeOff = 0;                          // 256 rows x 256 B
-constexpr uint32_t kThrRows = 255;                             // candidates stay <= 254
 constexpr uint32_t kLutThrOff = kLutDecodeOff + 256 * 256;     // 255 rows x 128 B
 constexpr uint32_t kStageOff = kLutThrOff + kThrRows * 128;    // [group][stage] x 16 KiB
 constexpr uint32_t kXchgOff = kStageOff + kGroups * kStages * kTileBytes;  // [group][ring][16] float4
@@ -97,8 +96,10 @@ struct TmaParams {
   uint32_t* errorFlag;  // set to 1 if a bounded wait gave up
 };
 
-__device__ __forceinline__ uint32_t smemAddr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+__device__ __forceinline__ Lut makeLut(uint32_t lane) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  const uint32_t base = smemAddr(smem);
+  return makeLutAt(base + kLutDecodeOff, base + kLutThrOff, lane);
 }
 
 __device__ __forceinline__ void groupSync(uint32_t g) {
@@ -132,129 +133,6 @@ __device__ __forceinline__ void tmaLoadRegion(uint32_t dst, const CUtensorMap* m
       "[%4];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
       : "memory");
-}
-
-__device__ __forceinline__ float lg2Approx(float x) {
-  float r;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-__device__ __forceinline__ float ex2Approx(float x) {
-  float r;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-
-// Lane constants for the replicated tables (shared-window addresses).
-struct Lut {
-  uint32_t decBase;   // the decode table
-  uint32_t laneWord;  // byte0 = 4*lane, byte1 = 4*lane + 128 (alpha half of a row)
-  uint32_t thrBase;   // threshold table + 4*lane - (0x4B400000 << 7)  (see encodeChannel)
-};
-
-__device__ __forceinline__ Lut makeLut(uint32_t lane) {
-  extern __shared__ __align__(128) uint8_t smem[];
-  const uint32_t base = smemAddr(smem);
-  Lut L;
-  L.decBase = base + kLutDecodeOff;
-  L.laneWord = (4 * lane) | ((4 * lane + 128) << 8);
-  L.thrBase = base + kLutThrOff + 4 * lane - (0x4B400000u << 7);
-  return L;
-}
-
-__device__ __forceinline__ float lds(uint32_t addr) {
-  float r;
-  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(r) : "r"(addr));
-  return r;
-}
-
-// NVPRO_PYRAMID_LOAD of one sRGBA8 texel: decode[r], decode[g], decode[b], alpha[a].
-__device__ __forceinline__ float4 decodeTexel(uint32_t w, const Lut& L) {
-  // PRMT builds (code << 8) | laneByte: row = code, column = this lane's copy.
-  return make_float4(lds(L.decBase + __byte_perm(w, L.laneWord, 0x6604)),
-                     lds(L.decBase + __byte_perm(w, L.laneWord, 0x6614)),
-                     lds(L.decBase + __byte_perm(w, L.laneWord, 0x6624)),
-                     lds(L.decBase + __byte_perm(w, L.laneWord, 0x6635)));
-}
-
-// Exact sRGB code of x in [0, 1], returned in the low byte.  With
-//   y  = 255 * OETF(x) + 0.5   (code = floor(y)),
-//   zp = 269.025 x^(5/12) - 14.925 = y - 1.4 on the power segment,
-//   zl = min(3294.6 x - 0.5, 9.4)  = y - 1   on the linear segment (capped),
-// z = max(zp, zl) lies in [y - 1.4, y - 1] up to ~1e-3, so a = rn(z) is code-1
-// or code, and code = a + (x >= threshold[a]).  z >= -0.5 (rounds to 0) and
-// z <= 254.1, so a indexes rows 0..254.  The magic add leaves a in the low
-// bits of `bits`, and (bits << 7) + thrBase is the address of threshold[a].
-__device__ __forceinline__ uint32_t encodeChannel(float x, const Lut& L) {
-  const float p = ex2Approx(lg2Approx(x) * 0.41666666f);
-  const float zp = fmaf(p, 269.025f, -14.925f);
-  const float zl = fminf(fmaf(x, 3294.6f, -0.5f), 9.4f);
-  const uint32_t bits = __float_as_uint(fmaxf(zp, zl) + 12582912.0f);
-  const float thr = lds(bits * 128u + L.thrBase);
-  return bits + (x >= thr ? 1u : 0u);
-}
-
-// srgbFromLinearVec's alpha: uint(a * 255 + 0.5) with truncation, via a
-// round-toward-zero add that leaves the integer in the low mantissa bits.
-__device__ __forceinline__ uint32_t encodeAlpha(float a) {
-  const float s = __fadd_rn(__fmul_rn(a, 255.0f), 0.5f);
-  return __float_as_uint(__fadd_rz(s, 8388608.0f));
-}
-
-// encodeChannel x3 + encodeAlpha with the independent multiplies and adds
-// paired into packed FP32 instructions (each lane of __fmul2_rn/__fadd2_rn/
-// __ffma2_rn rounds exactly like its scalar form, so the bytes are those of
-// the scalar functions).
-__device__ __forceinline__ uint32_t encodeTexel(float4 v, const Lut& L) {
-  constexpr float k = 0.41666666f, magic = 12582912.0f;
-  const float2 tRG = __fmul2_rn(make_float2(lg2Approx(v.x), lg2Approx(v.y)), make_float2(k, k));
-  const float2 tBa = __fmul2_rn(make_float2(lg2Approx(v.z), v.w), make_float2(k, 255.0f));  // (tB, a*255)
-  const float2 pRG = make_float2(ex2Approx(tRG.x), ex2Approx(tRG.y));
-  const float pB = ex2Approx(tBa.x);
-  const float2 zpRG = __ffma2_rn(pRG, make_float2(269.025f, 269.025f), make_float2(-14.925f, -14.925f));
-  // (zpB, a*255 + 0.5): the alpha add is exact-as-written (a*255*1 is exact)
-  const float2 zpBs = __ffma2_rn(make_float2(pB, tBa.y), make_float2(269.025f, 1.0f), make_float2(-14.925f, 0.5f));
-  const float2 zlRG = __ffma2_rn(make_float2(v.x, v.y), make_float2(3294.6f, 3294.6f), make_float2(-0.5f, -0.5f));
-  const float zlB = fmaf(v.z, 3294.6f, -0.5f);
-  const float2 mRG = __fadd2_rn(make_float2(fmaxf(zpRG.x, fminf(zlRG.x, 9.4f)), fmaxf(zpRG.y, fminf(zlRG.y, 9.4f))),
-                                make_float2(magic, magic));
-  const uint32_t bR = __float_as_uint(mRG.x), bG = __float_as_uint(mRG.y);
-  const uint32_t bB = __float_as_uint(fmaxf(zpBs.x, fminf(zlB, 9.4f)) + magic);
-  const uint32_t r = bR + (v.x >= lds(bR * 128u + L.thrBase) ? 1u : 0u);
-  const uint32_t g = bG + (v.y >= lds(bG * 128u + L.thrBase) ? 1u : 0u);
-  const uint32_t b = bB + (v.z >= lds(bB * 128u + L.thrBase) ? 1u : 0u);
-  const uint32_t a = __float_as_uint(__fadd_rz(zpBs.y, 8388608.0f));
-  return __byte_perm(__byte_perm(r, g, 0x0040), __byte_perm(b, a, 0x0040), 0x5410);
-}
-
-// REDUCE4 on packed pairs: 0.25 * ((v00 + v01) + (v10 + v11)) per channel,
-// same operations and order as reduce4().
-__device__ __forceinline__ float4 add4p(float4 a, float4 b) {
-  const float2 lo = __fadd2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
-  const float2 hi = __fadd2_rn(make_float2(a.z, a.w), make_float2(b.z, b.w));
-  return make_float4(lo.x, lo.y, hi.x, hi.y);
-}
-__device__ __forceinline__ float4 reduce4p(float4 v00, float4 v01, float4 v10, float4 v11) {
-  const float4 t = add4p(add4p(v00, v01), add4p(v10, v11));
-  const float2 lo = __fmul2_rn(make_float2(0.25f, 0.25f), make_float2(t.x, t.y));
-  const float2 hi = __fmul2_rn(make_float2(0.25f, 0.25f), make_float2(t.z, t.w));
-  return make_float4(lo.x, lo.y, hi.x, hi.y);
-}
-__device__ __forceinline__ float4 fastReduceP(bool vertical, float4 tl, float4 tr, float4 bl, float4 br) {
-  return vertical ? reduce4p(tl, bl, tr, br) : reduce4p(tl, tr, bl, br);
-}
-
-__device__ __forceinline__ float4 shflXor(float4 v, int m) {
-  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
-                     __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
-}
-__device__ __forceinline__ float4 shflDown(float4 v, int d) {
-  return make_float4(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
-                     __shfl_down_sync(0xffffffffu, v.z, d), __shfl_down_sync(0xffffffffu, v.w, d));
-}
-__device__ __forceinline__ float4 shflUp(float4 v, int d) {
-  return make_float4(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d),
-                     __shfl_up_sync(0xffffffffu, v.z, d), __shfl_up_sync(0xffffffffu, v.w, d));
 }
 
 __device__ __forceinline__ uint32_t* texelPtr(const FusedStage& st, uint32_t k, uint32_t x, uint32_t y) {
@@ -553,14 +431,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ __align__(128) uint8_t smem[];
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  float* lutDec = reinterpret_cast<float*>(smem + kLutDecodeOff);
-  float* lutThr = reinterpret_cast<float*>(smem + kLutThrOff);
-  for (uint32_t i = tid; i < 256 * 32; i += kThreads) {
-    const uint32_t code = i >> 5, l = i & 31;
-    lutDec[code * 64 + l] = __uint_as_float(c_srgbDecodeBits[code]);
-    lutDec[code * 64 + 32 + l] = __uint_as_float(c_alphaDecodeBits[code]);
-    if (code < kThrRows) lutThr[code * 32 + l] = __uint_as_float(c_srgbThresholdBits[code]);
-  }
+  fillLut(reinterpret_cast<float*>(smem + kLutDecodeOff), reinterpret_cast<float*>(smem + kLutThrOff), tid,
+          kThreads);
   if (tid == 0) {
     for (uint32_t g = 0; g < kGroups; ++g) {
       const GroupCtx G = groupCtx(g);
@@ -635,7 +507,11 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // Encode every float of x (test support for the exhaustive codec check).
-__global__ void debugEncodeKernel(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n) {
+// alpha = 0: the value goes through the packed texel encoder as colour
+// channel i % 3, with its neighbours in the array as the other channels, and
+// `exact` is the threshold count; alpha = 1: the value is the texel's alpha
+// and `exact` is the scalar alphaEncode.
+__global__ void debugEncodeKernel(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, uint32_t alpha) {
   extern __shared__ __align__(128) uint8_t smem[];
   float* lutThr = reinterpret_cast<float*>(smem + kLutThrOff);
   __shared__ float full[256];
@@ -648,10 +524,13 @@ __global__ void debugEncodeKernel(const float* x, uint8_t* fast, uint8_t* exact,
     const float v = x[i];
     // The fast encoder's table index is derived from the value; keep it in
     // the encoder's domain [0, 1] (NaN -> 0) whatever the caller passes.
-    // The value goes through the packed texel encoder in channel i % 3, with
-    // its neighbours in the array as the other channels.
     auto dom = [](float f) { return fminf(fmaxf(f, 0.0f), 1.0f); };
     const float u = dom(x[(i + 1) % n]), w = dom(x[(i + 2) % n]), cv = dom(v);
+    if (alpha) {
+      fast[i] = uint8_t(encodeTexel(make_float4(u, w, u, cv), L) >> 24);
+      exact[i] = uint8_t(alphaEncode(cv));
+      continue;
+    }
     const uint32_t ch = uint32_t(i % 3);
     const float4 t = ch == 0 ? make_float4(cv, u, w, 0.5f) : ch == 1 ? make_float4(u, cv, w, 0.5f)
                                                                     : make_float4(u, w, cv, 0.5f);
@@ -817,11 +696,12 @@ cudaError_t staticScratch(uint32_t** ptr) {
   return cudaSuccess;
 }
 
-cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, cudaStream_t stream) {
+cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, uint32_t alpha,
+                              cudaStream_t stream) {
   DeviceInfo* info = nullptr;
   cudaError_t e = deviceInfo(&info);
   if (e != cudaSuccess) return e;
-  debugEncodeKernel<<<info->sms * 2, 256, kDebugSmemBytes, stream>>>(x, fast, exact, n);
+  debugEncodeKernel<<<info->sms * 2, 256, kDebugSmemBytes, stream>>>(x, fast, exact, n, alpha);
   return cudaGetLastError();
 }
 
