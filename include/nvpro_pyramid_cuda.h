@@ -322,6 +322,63 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerateNoAlloc(
     NvproPyramidStream stream, NvproPyramidPreset preset, const NvproPyramidImage* pImage,
     uint32_t mipLevels);
 
+/* ------------------------------------------------------------------------ */
+/* Batches (no reference counterpart: the reference records one chain per   */
+/* command buffer, nvpro_pyramid_dispatch.hpp:109-188, and its benchmark     */
+/* submits images one at a time, demo_app/mipmaps_app.cpp:666-767).         */
+/*                                                                          */
+/* A batch generates the full default chain of many sRGBA8 images of any    */
+/* sizes in one persistent kernel launch: phase k runs the k-th dispatch of */
+/* every image's schedule, warps take work units from a per-phase queue,    */
+/* and a grid barrier separates phases.  The bytes equal those of           */
+/* nvproPyramidGenerate on each image.                                       */
+/* ------------------------------------------------------------------------ */
+
+typedef struct NvproPyramidBatch_T* NvproPyramidBatch;
+
+/* Build flags. */
+#define NVPRO_PYRAMID_BATCH_AUTOTUNE 1u /* pick the work-unit size by timing candidates,
+                                           cached per size class of the batch */
+#define NVPRO_PYRAMID_BATCH_GRAPH 2u    /* launches replay a CUDA graph captured at build */
+
+typedef struct NvproPyramidBatchInfo {
+  uint32_t imageCount;
+  uint32_t phaseCount; /* dispatches of the longest schedule */
+  uint32_t jobCount;   /* dispatches over all images */
+  uint32_t stripBand;  /* rows of level L+2 per general-pipeline work unit */
+  uint64_t unitCount;  /* work units over all phases */
+  uint32_t autotuned;  /* stripBand chosen by the autotuner */
+  uint32_t fromCache;  /* ... from the cache of an earlier build of the same size class */
+  uint32_t graph;      /* launches replay a CUDA graph */
+  uint32_t reserved;
+} NvproPyramidBatchInfo;
+
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCreateBatch(NvproPyramidPreset preset, uint32_t flags,
+                                                             NvproPyramidBatch* pBatch);
+NVPRO_PYRAMID_API void nvproPyramidDestroyBatch(NvproPyramidBatch batch);
+
+/* Plan the batch for `images` (each with its levels bound as for
+ * nvproPyramidGenerate; mipLevels as there, 0 = each image's full chain) and
+ * copy the plan to device memory that the batch owns.  With
+ * NVPRO_PYRAMID_BATCH_AUTOTUNE and a size class not seen before, this runs
+ * the batch a few times on `stream` (writing the images' levels) and waits
+ * for it.  The image memory must stay valid while the batch is launched. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch batch, NvproPyramidStream stream,
+                                                            const NvproPyramidImage* images,
+                                                            uint32_t imageCount, uint32_t mipLevels);
+
+/* Generate levels 1.. of every image of the batch on `stream` (no
+ * allocation, no host synchronisation).  Launches of one batch must not
+ * overlap on the GPU: they share the batch's work counters. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchLaunch(NvproPyramidBatch batch, NvproPyramidStream stream);
+
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchGetInfo(NvproPyramidBatch batch,
+                                                              NvproPyramidBatchInfo* info);
+
+/* Wait for the device, then report NVPRO_PYRAMID_ERROR_TIMEOUT if a bounded
+ * grid-barrier wait of a launch of this batch gave up since the last query. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchDeviceStatus(NvproPyramidBatch batch);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -6,13 +6,14 @@ include/nvpro_pyramid_cuda.h, CUDA kernels for sm_103a).  This package loads
 it through ctypes and adds torch conveniences; it has no CPU fallback.
 """
 from . import _native
-from ._native import (CMD_NO_FUSION, CMD_PORTABLE_KERNELS, CMD_RECORD_ONLY, PRESET_RGBA16F, PRESET_RGBA32F,
-                      PRESET_SRGBA8, NativeLibraryError, NvproPyramidImage, NvproPyramidState)
-from .pyramid import (Cmd, MipChain, Pipelines, cmd_pyramid_dispatch, full_level_count, generate, level_sizes,
-                      make_image, packed_offsets, wrap_dispatcher)
+from ._native import (BATCH_AUTOTUNE, BATCH_GRAPH, CMD_NO_FUSION, CMD_PORTABLE_KERNELS, CMD_RECORD_ONLY,
+                      PRESET_RGBA16F, PRESET_RGBA32F, PRESET_SRGBA8, NativeLibraryError, NvproPyramidImage,
+                      NvproPyramidState)
+from .pyramid import (Batch, Cmd, MipChain, Pipelines, cmd_pyramid_dispatch, full_level_count, generate,
+                      level_sizes, make_image, pack_chains, packed_offsets, wrap_dispatcher)
 
 __all__ = [
-    "CMD_NO_FUSION", "CMD_PORTABLE_KERNELS", "CMD_RECORD_ONLY", "PRESET_RGBA16F", "PRESET_RGBA32F",
+    "BATCH_AUTOTUNE", "BATCH_GRAPH", "Batch", "pack_chains", "CMD_NO_FUSION", "CMD_PORTABLE_KERNELS", "CMD_RECORD_ONLY", "PRESET_RGBA16F", "PRESET_RGBA32F",
     "PRESET_SRGBA8", "NativeLibraryError", "NvproPyramidImage", "NvproPyramidState", "Cmd", "MipChain",
     "Pipelines", "cmd_pyramid_dispatch", "full_level_count", "generate", "level_sizes", "make_image",
     "packed_offsets", "wrap_dispatcher",

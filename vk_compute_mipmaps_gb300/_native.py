@@ -74,6 +74,23 @@ class NvproPyramidDispatchRecord(ctypes.Structure):
     ]
 
 
+class NvproPyramidBatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("imageCount", c_uint32),
+        ("phaseCount", c_uint32),
+        ("jobCount", c_uint32),
+        ("stripBand", c_uint32),
+        ("unitCount", c_uint64),
+        ("autotuned", c_uint32),
+        ("fromCache", c_uint32),
+        ("graph", c_uint32),
+        ("reserved", c_uint32),
+    ]
+
+
+BATCH_AUTOTUNE = 1
+BATCH_GRAPH = 2
+
 # nvpro_pyramid_dispatcher_t
 DISPATCHER = ctypes.CFUNCTYPE(c_uint32, c_void_p, c_void_p, c_uint32, c_void_p, POINTER(NvproPyramidState))
 
@@ -112,6 +129,12 @@ SIGNATURES = {
     "nvproPyramidCmdDeviceStatus": (c_int, [c_void_p]),
     "nvproPyramidDebugSrgbEncode": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
     "nvproPyramidDebugAlphaEncode": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint64]),
+    "nvproPyramidCreateBatch": (c_int, [c_int, c_uint32, POINTER(c_void_p)]),
+    "nvproPyramidDestroyBatch": (None, [c_void_p]),
+    "nvproPyramidBatchBuild": (c_int, [c_void_p, c_void_p, POINTER(NvproPyramidImage), c_uint32, c_uint32]),
+    "nvproPyramidBatchLaunch": (c_int, [c_void_p, c_void_p]),
+    "nvproPyramidBatchGetInfo": (c_int, [c_void_p, POINTER(NvproPyramidBatchInfo)]),
+    "nvproPyramidBatchDeviceStatus": (c_int, [c_void_p]),
     "nvproPyramidAdjointWorkspaceBytes": (c_uint64, [c_uint32, c_uint32, c_uint32]),
     "nvproPyramidAdjoint": (c_int, [c_void_p, c_int, POINTER(NvproPyramidImage), c_void_p, c_uint64, c_uint32,
                                     c_void_p, c_uint64]),

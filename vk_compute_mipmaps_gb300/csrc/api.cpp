@@ -13,11 +13,14 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "../../include/nvpro_pyramid_cuda.h"
+#include "batch.h"
 #include "internal.h"
 
 using namespace nvpyr;
@@ -598,6 +601,41 @@ uint32_t defaultSchedule(uint32_t w, uint32_t h, uint32_t mipLevels, SchedEntry*
   return n;
 }
 
+// The default schedule of one image (nvpro_pyramid_dispatch.hpp:109-304 with
+// both pipelines: nvproPyramidDefaultFastDispatcher<4, 6>, else
+// nvproPyramidDefaultGeneralDispatcher) as launch parameters, in a
+// caller-provided array of NVPRO_PYRAMID_MAX_LEVELS entries.
+NvproPyramidResult defaultParams(NvproPyramidPreset preset, const NvproPyramidImage* pImage, uint32_t mipLevels,
+                                 DispatchParams* params, uint32_t* count) {
+  *count = 0;
+  if (!pImage) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pImage is NULL");
+  if (presetBytes(uint32_t(preset)) == 0)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "unknown preset %d", int(preset));
+  const uint32_t w = pImage->width, h = pImage->height;
+  if (w == 0 || h == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "zero width or height");
+  const uint32_t full = nvproPyramidFullLevelCount(w, h);
+  if (mipLevels == 0) mipLevels = full;
+  if (mipLevels > full || mipLevels > NVPRO_PYRAMID_MAX_LEVELS || pImage->levelCount < mipLevels)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u levels requested; %ux%u image binds %u of at most %u",
+                mipLevels, w, h, pImage->levelCount, full);
+  Record rec;
+  std::memset(&rec, 0, sizeof rec);
+  rec.image = *pImage;
+  rec.info.preset = uint32_t(preset);
+  rec.info.groupCountY = rec.info.groupCountZ = 1;
+  SchedEntry sched[NVPRO_PYRAMID_MAX_LEVELS];
+  const uint32_t n = defaultSchedule(w, h, mipLevels, sched);
+  for (uint32_t i = 0; i < n; ++i) {
+    rec.info.isFastPipeline = sched[i].isFast;
+    rec.info.pushConstant = sched[i].level << NVPRO_PYRAMID_INPUT_LEVEL_SHIFT | sched[i].count;
+    rec.info.groupCountX = sched[i].groups;
+    NvproPyramidResult r = makeParams(rec, &params[i]);
+    if (r != NVPRO_PYRAMID_SUCCESS) return r;
+  }
+  *count = n;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
 // Levels whose adjoint values the sweep materialises in the workspace (all
 // input levels of dispatches except 0, and the middle level of 2-level
 // general dispatches), with their byte offsets.
@@ -741,56 +779,12 @@ NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPr
 
 NvproPyramidResult nvproPyramidGenerateNoAlloc(NvproPyramidStream stream, NvproPyramidPreset preset,
                                                const NvproPyramidImage* pImage, uint32_t mipLevels) {
-  // The default schedule (nvpro_pyramid_dispatch.hpp:109-304 with both
-  // pipelines) is built in fixed-size stack arrays: no command object, no
-  // device or host allocation on the way to the launches.
-  if (!pImage) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pImage is NULL");
-  if (presetBytes(uint32_t(preset)) == 0)
-    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "unknown preset %d", int(preset));
-  const uint32_t w = pImage->width, h = pImage->height;
-  if (w == 0 || h == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "zero width or height");
-  const uint32_t full = nvproPyramidFullLevelCount(w, h);
-  if (mipLevels == 0) mipLevels = full;
-  if (mipLevels > full || mipLevels > NVPRO_PYRAMID_MAX_LEVELS || pImage->levelCount < mipLevels)
-    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u levels requested; %ux%u image binds %u of at most %u",
-                mipLevels, w, h, pImage->levelCount, full);
-  Record rec;
-  std::memset(&rec, 0, sizeof rec);
-  rec.image = *pImage;
-  rec.info.preset = uint32_t(preset);
-  rec.info.groupCountY = rec.info.groupCountZ = 1;
+  // The default schedule is built in fixed-size stack arrays: no command
+  // object, no device or host allocation on the way to the launches.
   DispatchParams params[NVPRO_PYRAMID_MAX_LEVELS];
   uint32_t count = 0;
-  NvproPyramidState st{0u, mipLevels - 1u, w, h};
-  while (st.remainingLevels != 0) {
-    uint32_t done = 0, groups = 0;
-    bool fast = false;
-    if (st.currentX % 4 == 0 && st.currentY % 4 == 0) {  // nvproPyramidDefaultFastDispatcher<4, 6>
-      uint32_t x = st.currentX, y = st.currentY;
-      while (x % 2 == 0 && y % 2 == 0 && done < st.remainingLevels && done < 6) {
-        x /= 2;
-        y /= 2;
-        ++done;
-      }
-      fast = true;
-      const uint32_t shift = done > 5 ? 12u : 10u, mask = done > 5 ? 4095u : 1023u;
-      groups = (st.currentX * st.currentY + mask) >> shift;
-    } else {  // nvproPyramidDefaultGeneralDispatcher
-      done = st.remainingLevels >= 2 ? 2u : st.remainingLevels;
-      const uint32_t dw = std::max(st.currentX >> done, 1u), dh = std::max(st.currentY >> done, 1u);
-      groups = done == 1 ? (dw * dh + 127) / 128 : ((dw + 7) / 8) * ((dh + 7) / 8);
-    }
-    rec.info.isFastPipeline = fast;
-    rec.info.pushConstant = st.currentLevel << NVPRO_PYRAMID_INPUT_LEVEL_SHIFT | done;
-    rec.info.groupCountX = groups;
-    NvproPyramidResult r = makeParams(rec, &params[count]);
-    if (r != NVPRO_PYRAMID_SUCCESS) return r;
-    ++count;
-    st.currentLevel += done;
-    st.remainingLevels -= done;
-    st.currentX = std::max(st.currentX >> done, 1u);
-    st.currentY = std::max(st.currentY >> done, 1u);
-  }
+  NvproPyramidResult r = defaultParams(preset, pImage, mipLevels, params, &count);
+  if (r != NVPRO_PYRAMID_SUCCESS) return r;
   if (count == 0) return NVPRO_PYRAMID_SUCCESS;
 
   uint32_t* scratch = nullptr;
@@ -841,6 +835,254 @@ NvproPyramidResult nvproPyramidGenerate(NvproPyramidCmd cmd, NvproPyramidStream 
   nvproPyramidCmdBindImage(cmd, pImage);
   if (pImage) nvproCmdPyramidDispatch(cmd, pipelines, pImage->width, pImage->height, mipLevels);
   return nvproPyramidEndCmd(cmd);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches (no reference counterpart): many images, one persistent launch.
+
+namespace {
+
+constexpr uint32_t kBatchMagic = 0x4E50424Du;  // 'NPBM'
+constexpr uint32_t kBandCandidates[] = {4, 8, 16, 32};
+constexpr uint32_t kDefaultStripBand = 8;
+
+// Autotuner cache: strip band by size class (device, mip levels and the
+// histogram of log2(max side) over the batch, counts rounded to powers of two).
+std::mutex g_tuneMu;
+std::map<std::string, uint32_t> g_tuneCache;
+
+std::string sizeClassKey(const NvproPyramidImage* images, uint32_t count, uint32_t mipLevels) {
+  uint32_t hist[32] = {};
+  for (uint32_t i = 0; i < count; ++i) {
+    uint32_t m = std::max(images[i].width, images[i].height), b = 0;
+    while (m >>= 1) ++b;
+    ++hist[b];
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::string key = std::to_string(dev) + ":" + std::to_string(mipLevels) + ":";
+  for (uint32_t b = 0; b < 32; ++b) {
+    uint32_t c = hist[b], r = 0;
+    while (c) {
+      c >>= 1;
+      ++r;
+    }
+    key += char('a' + r);
+  }
+  return key;
+}
+
+}  // namespace
+
+struct NvproPyramidBatch_T {
+  uint32_t magic = kBatchMagic;
+  NvproPyramidPreset preset = NVPRO_PYRAMID_PRESET_SRGBA8;
+  uint32_t flags = 0;
+  nvpyr::BatchPlan plan;
+  nvpyr::BatchDevice dev;
+  void* devMem = nullptr;
+  uint64_t devBytes = 0;
+  uint32_t imageCount = 0;
+  uint32_t stripBand = kDefaultStripBand;
+  uint32_t autotuned = 0, fromCache = 0;
+  cudaStream_t captureStream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool built = false;
+
+  void dropGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+  ~NvproPyramidBatch_T() {
+    dropGraph();
+    if (captureStream) cudaStreamDestroy(captureStream);
+    if (devMem) cudaFree(devMem);
+    magic = 0;
+  }
+  // plan with `band` and copy it to the device block (grown if needed)
+  cudaError_t planAndUpload(const std::vector<std::vector<DispatchParams>>& imgs, uint32_t band, cudaStream_t s) {
+    cudaError_t e = plan.build(imgs, band);
+    if (e != cudaSuccess) return e;
+    const uint64_t need = plan.deviceBytes();
+    if (need > devBytes) {
+      if (devMem) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        cudaFree(devMem);
+        devMem = nullptr;
+        devBytes = 0;
+      }
+      e = cudaMalloc(&devMem, need);
+      if (e != cudaSuccess) return e;
+      devBytes = need;
+      e = cudaMemset(devMem, 0, need);  // the error flag starts clear
+      if (e != cudaSuccess) return e;
+    }
+    return plan.upload(devMem, s, &dev);
+  }
+};
+
+namespace {
+bool validBatch(NvproPyramidBatch b) { return b && b->magic == kBatchMagic; }
+}  // namespace
+
+extern "C" {
+
+NvproPyramidResult nvproPyramidCreateBatch(NvproPyramidPreset preset, uint32_t flags, NvproPyramidBatch* pBatch) {
+  if (!pBatch) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pBatch is NULL");
+  *pBatch = nullptr;
+  if (preset != NVPRO_PYRAMID_PRESET_SRGBA8)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "batches exist for the sRGBA8 preset only");
+  if (flags & ~(NVPRO_PYRAMID_BATCH_AUTOTUNE | NVPRO_PYRAMID_BATCH_GRAPH))
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "unknown batch flags 0x%x", flags);
+  auto* b = new (std::nothrow) NvproPyramidBatch_T;
+  if (!b) return fail(NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY, "batch object");
+  b->preset = preset;
+  b->flags = flags;
+  *pBatch = b;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+void nvproPyramidDestroyBatch(NvproPyramidBatch batch) {
+  if (validBatch(batch)) delete batch;
+}
+
+NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch b, NvproPyramidStream stream,
+                                          const NvproPyramidImage* images, uint32_t imageCount,
+                                          uint32_t mipLevels) {
+  if (!validBatch(b)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid batch object");
+  if (!images && imageCount) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "images is NULL");
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  b->built = false;
+  b->dropGraph();
+  std::vector<std::vector<DispatchParams>> imgs(imageCount);
+  for (uint32_t i = 0; i < imageCount; ++i) {
+    DispatchParams params[NVPRO_PYRAMID_MAX_LEVELS];
+    uint32_t count = 0;
+    NvproPyramidResult r = defaultParams(b->preset, &images[i], mipLevels, params, &count);
+    if (r != NVPRO_PYRAMID_SUCCESS) return r;
+    imgs[i].assign(params, params + count);
+  }
+  b->imageCount = imageCount;
+  b->autotuned = b->fromCache = 0;
+  uint32_t band = kDefaultStripBand;
+  cudaError_t e = cudaSuccess;
+  if (b->flags & NVPRO_PYRAMID_BATCH_AUTOTUNE) {
+    const std::string key = sizeClassKey(images, imageCount, mipLevels);
+    bool cached = false;
+    {
+      std::lock_guard<std::mutex> lock(g_tuneMu);
+      auto it = g_tuneCache.find(key);
+      if (it != g_tuneCache.end()) {
+        band = it->second;
+        cached = true;
+      }
+    }
+    if (!cached) {
+      // Time each candidate on `stream` (a warm-up run, then the median of
+      // three) -- the real work, writing the images' levels.
+      float best = 0;
+      cudaEvent_t ev[2];
+      e = cudaEventCreate(&ev[0]);
+      if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+      for (uint32_t c : kBandCandidates) {
+        if (e != cudaSuccess) break;
+        e = b->planAndUpload(imgs, c, s);
+        uint32_t launches = 0;
+        float t[3] = {};
+        for (int it = 0; it < 4 && e == cudaSuccess; ++it) {
+          if (it > 0) e = cudaEventRecord(ev[0], s);
+          if (e == cudaSuccess) e = nvpyr::launchBatch(b->dev, s, &launches);
+          if (e == cudaSuccess && it > 0) e = cudaEventRecord(ev[1], s);
+          if (e == cudaSuccess && it > 0) e = cudaEventSynchronize(ev[1]);
+          if (e == cudaSuccess && it > 0) e = cudaEventElapsedTime(&t[it - 1], ev[0], ev[1]);
+        }
+        std::sort(t, t + 3);
+        if (e == cudaSuccess && (best == 0 || t[1] < best)) {
+          best = t[1];
+          band = c;
+        }
+      }
+      cudaEventDestroy(ev[0]);
+      cudaEventDestroy(ev[1]);
+      if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "batch autotune: %s", cudaGetErrorString(e));
+      std::lock_guard<std::mutex> lock(g_tuneMu);
+      g_tuneCache[key] = band;
+    }
+    b->autotuned = 1;
+    b->fromCache = cached ? 1 : 0;
+  }
+  b->stripBand = band;
+  e = b->planAndUpload(imgs, band, s);
+  if (e == cudaErrorInvalidValue)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "a dispatch of the batch is not supported by the batch kernel");
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "batch tables: %s", cudaGetErrorString(e));
+  if (b->flags & NVPRO_PYRAMID_BATCH_GRAPH) {
+    // Capture the launch (counter reset + kernel) once; launches replay it.
+    e = nvpyr::batchDeviceReady();
+    if (e == cudaSuccess && !b->captureStream) e = cudaStreamCreateWithFlags(&b->captureStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(b->captureStream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      uint32_t launches = 0;
+      const cudaError_t le = nvpyr::launchBatch(b->dev, b->captureStream, &launches);
+      e = cudaStreamEndCapture(b->captureStream, &b->graph);
+      if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e != cudaSuccess) {
+      b->dropGraph();
+      return fail(NVPRO_PYRAMID_ERROR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+    }
+  }
+  b->built = true;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidBatchLaunch(NvproPyramidBatch b, NvproPyramidStream stream) {
+  if (!validBatch(b)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid batch object");
+  if (!b->built) return fail(NVPRO_PYRAMID_ERROR_INVALID_STATE, "batch is not built");
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (b->exec) {
+    e = cudaGraphLaunch(b->exec, s);
+  } else {
+    uint32_t launches = 0;
+    e = nvpyr::launchBatch(b->dev, s, &launches);
+  }
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "batch launch: %s", cudaGetErrorString(e));
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidBatchGetInfo(NvproPyramidBatch b, NvproPyramidBatchInfo* info) {
+  if (!validBatch(b) || !info) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid batch or info");
+  std::memset(info, 0, sizeof *info);
+  info->imageCount = b->imageCount;
+  info->phaseCount = b->plan.phaseCount();
+  info->jobCount = b->plan.jobCount();
+  info->stripBand = b->stripBand;
+  info->unitCount = b->plan.unitCount();
+  info->autotuned = b->autotuned;
+  info->fromCache = b->fromCache;
+  info->graph = b->exec ? 1u : 0u;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidBatchDeviceStatus(NvproPyramidBatch b) {
+  if (!validBatch(b)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid batch object");
+  if (!b->built || !b->dev.counters) return NVPRO_PYRAMID_SUCCESS;
+  cudaError_t e = cudaDeviceSynchronize();
+  uint32_t flag = 0;
+  uint8_t* at = reinterpret_cast<uint8_t*>(b->dev.counters) + b->plan.errorFlagOffset();
+  if (e == cudaSuccess) e = cudaMemcpy(&flag, at, sizeof flag, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && flag) e = cudaMemset(at, 0, sizeof flag);
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "batch status: %s", cudaGetErrorString(e));
+  if (flag) return fail(NVPRO_PYRAMID_ERROR_TIMEOUT, "a bounded device wait of the batch kernel gave up");
+  return NVPRO_PYRAMID_SUCCESS;
 }
 
 }  // extern "C"

@@ -3,24 +3,7 @@
 // dispatch, as warp-wide column strips that stream down the image, and a run
 // of consecutive general dispatches in one persistent launch.
 //
-// Work decomposition.  A unit of work is one warp's strip: a band of rows of
-// the last level of the dispatch, 15 columns of level L+2 (two levels) or 31
-// columns of level L+1 (one level).  Lane l owns level-(L+1) column
-// x = x0 + l and loads level-L columns 2x and 2x+1; a three-tap column 2x+2
-// is lane l+1's first column (shfl.down 1).  The warp walks the band's
-// level-(L+1) rows top to bottom: each row reads two new level-L rows (the
-// third row of a three-tap window is the previous row's last), reduces them
-// vertically per column, then horizontally across lanes (vertical first, as
-// reduceStoreSample_ does, :588-651), stores the encoded texel, and keeps the
-// FP32 value for level L+2, which reduces the same way over the lanes'
-// level-(L+1) rows (fillLastTile_ reads FP32 level L+1 from shared memory,
-// :790-820; here it comes from registers).  The level-L rows of the next four
-// level-(L+1) rows are in flight while the current four are reduced.
-//
-// Every texel's value depends only on its inputs and the fixed operation
-// order, so strips overlap by one level-(L+1) column / row where a three-tap
-// window crosses a strip edge; the overlapping texels are recomputed and
-// stored by one strip only.  The results equal the portable kernels' bytes.
+// The strips themselves are described in general_strip.cuh.
 //
 // Chains.  The dispatches of a run are the stages of one cooperative launch
 // (all CTAs resident): the sRGB tables are filled once, and a grid barrier
@@ -30,7 +13,7 @@
 // returns.
 #include <mutex>
 
-#include "srgb_codec.cuh"
+#include "general_strip.cuh"
 
 namespace nvpyr {
 namespace {
@@ -39,32 +22,8 @@ constexpr uint32_t kWarps = 16;
 constexpr uint32_t kThreads = 32 * kWarps;
 constexpr uint32_t kCtasPerSm = 1;
 constexpr uint32_t kMaxStages = 16;
-constexpr uint32_t kWaitLimit = 1u << 22;  // barrier polls (with backoff: about a second)
-// The decode table sits at the first 64 KiB boundary of the shared window at
-// or after the dynamic block, the threshold table below it if it fits there,
-// else above it: 128 KiB cover every placement.
-constexpr uint32_t kSmemBytes = 2 * kLutDecodeBytes;
-constexpr uint32_t kCols2 = 15;     // level-(L+2) columns per strip (two levels)
-constexpr uint32_t kCols1 = 31;     // level-(L+1) columns per strip (one level)
-constexpr uint32_t kGroupRows = 4;  // level-(L+1) rows whose level-L rows load together
+constexpr uint32_t kSmemBytes = kAlignedLutSmemBytes;
 static_assert(kCtasPerSm * (kSmemBytes + 1024u) <= 228u * 1024u, "the CTAs of an SM must fit");
-
-// One dispatch (a stage of a chain launch).
-struct Stage {
-  const uint8_t* src;
-  uint64_t srcPitch;
-  uint32_t w0, h0;
-  uint8_t* dst1;
-  uint64_t pitch1;
-  uint32_t w1, h1;
-  uint8_t* dst2;
-  uint64_t pitch2;
-  uint32_t w2, h2;
-  uint32_t tilesX;   // strips across the last level
-  uint32_t bands;    // bands down the last level
-  uint32_t band;     // rows of the last level per band
-  uint32_t variant;  // two levels: tx0<<3 | ty0<<2 | tx1<<1 | ty1; one level: 16 + (tx0<<1 | ty0)
-};
 
 struct ChainParams {
   Stage st[kMaxStages];
@@ -74,252 +33,8 @@ struct ChainParams {
   uint32_t* errorFlag;     // set to 1 if a bounded wait gave up
 };
 
-// REDUCE / REDUCE2 (srgba8_mipmap_preamble.glsl:24-38), equal to reduce3() /
-// reduce2(): products on packed pairs (__fmul2_rn), sums with __fadd_rn.  The
-// sums must stay scalar: __fadd_rn is never merged into a multiply-add, while
-// packed adds next to packed multiplies were seen fused (a fused
-// w0*v0 + w1*v1 changes encoded bytes).
-__device__ __forceinline__ float4 mul4p(float s, float4 a) {
-  const float2 lo = __fmul2_rn(make_float2(s, s), make_float2(a.x, a.y));
-  const float2 hi = __fmul2_rn(make_float2(s, s), make_float2(a.z, a.w));
-  return make_float4(lo.x, lo.y, hi.x, hi.y);
-}
-__device__ __forceinline__ float4 reduce3p(const Weights3& w, float4 v0, float4 v1, float4 v2) {
-  return f4add(f4add(mul4p(w.w0, v0), mul4p(w.w1, v1)), mul4p(w.w2, v2));
-}
-__device__ __forceinline__ float4 reduce2p(float4 v0, float4 v1) { return mul4p(0.5f, f4add(v0, v1)); }
-
-// weights3(n, i) with the reciprocal 1 / (2n + 1) computed once per level.
-struct Axis3 {
-  float nf, rcp;
-};
-__device__ __forceinline__ Axis3 axis3(uint32_t n) {
-  const float nf = __uint2float_rn(n);
-  return Axis3{nf, __frcp_rn(__fadd_rn(__fmul_rn(2.0f, nf), 1.0f))};
-}
-__device__ __forceinline__ Weights3 weightsAt(const Axis3& a, uint32_t i) {
-  Weights3 w;
-  w.w0 = __fmul_rn(a.rcp, __fsub_rn(a.nf, __uint2float_rn(i)));
-  w.w1 = __fmul_rn(a.rcp, a.nf);
-  w.w2 = __fsub_rn(__fsub_rn(1.0f, w.w0), w.w1);
-  return w;
-}
-
-// Texel load, cached in L1 (the second of a lane's two columns hits the
-// sector the first one fetched).  L1 is not coherent across SMs, but a level
-// is only ever read after the grid barrier that follows its last write, and
-// no SM reads it before that, so no SM can hold a stale line of it.  Volatile
-// keeps the prefetch ahead of the table lookups.
-__device__ __forceinline__ uint32_t ldTexel(const uint8_t* p) {
-  uint32_t v;
-  asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(v) : "l"(p));
-  return v;
-}
-
-// decodeTexel for a decode table at a 64 KiB-aligned shared address: the
-// PRMT builds the whole address, table bytes 2-3 coming from laneWord.
-__device__ __forceinline__ float4 decodeAligned(uint32_t w, const Lut& L) {
-  return make_float4(lds(__byte_perm(w, L.laneWord, 0x7604)), lds(__byte_perm(w, L.laneWord, 0x7614)),
-                     lds(__byte_perm(w, L.laneWord, 0x7624)), lds(__byte_perm(w, L.laneWord, 0x7635)));
-}
-
-// One strip of a one- or two-level dispatch.  TX0 / TY0: three-tap kernel
-// from level L along x / y (else two taps); TX1 / TY1: the same from level
-// L+1 (two levels only).  The flags are uniform across the grid, so their
-// branches never diverge; one code path for all of them keeps the chain
-// kernel free of calls.
-__device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t band, uint32_t lane, const Lut& lut) {
-  const uint32_t LEVELS = st.variant >= 16 ? 1u : 2u;
-  const bool TX0 = LEVELS == 2 ? (st.variant & 8) != 0 : (st.variant & 2) != 0;
-  const bool TY0 = LEVELS == 2 ? (st.variant & 4) != 0 : (st.variant & 1) != 0;
-  const bool TX1 = LEVELS == 2 && (st.variant & 2) != 0;
-  const bool TY1 = LEVELS == 2 && (st.variant & 1) != 0;
-  // Every field in a register before the first store: stores through
-  // generic pointers would otherwise force reloads of a stage held in memory.
-  const Lut L = lut;
-  struct {
-    const uint8_t* src;
-    uint64_t srcPitch;
-    uint32_t w0, h0;
-    uint8_t* dst1;
-    uint64_t pitch1;
-    uint32_t w1, h1;
-    uint8_t* dst2;
-    uint64_t pitch2;
-    uint32_t w2, h2, band;
-  } const p = {st.src, st.srcPitch, st.w0, st.h0, st.dst1, st.pitch1, st.w1, st.h1, st.dst2, st.pitch2, st.w2, st.h2,
-               st.band};
-  const uint32_t cols = LEVELS == 2 ? 2 * kCols2 : kCols1;  // level-(L+1) columns owned by a strip
-  const uint32_t x0 = tile * cols;
-  const uint32_t x = x0 + lane;
-  // level-L columns of this lane, clamped into the level for lanes past its edge
-  const uint8_t* colA = p.src + uint64_t(min(2 * x, p.w0 - 1)) * 4;
-  const uint8_t* colB = p.src + uint64_t(min(2 * x + 1, p.w0 - 1)) * 4;
-  const Axis3 ax1 = axis3(p.w1), ay1 = axis3(p.h1);
-  const Weights3 wx = weightsAt(ax1, min(x, p.w1 - 1));
-
-  // rows [yb, ye) of level L+1, of which [yb, yStoreEnd) are this strip's
-  uint32_t yb, ye, yStoreEnd;
-  bool store1x;
-  if (LEVELS == 2) {
-    const uint32_t Yb = band * p.band, Ye = min(Yb + p.band, p.h2);
-    yb = 2 * Yb;
-    ye = 2 * Ye + (TY1 ? 1 : 0);
-    yStoreEnd = Ye == p.h2 ? p.h1 : 2 * Ye;
-    const bool lastTile = (tile + 1) * kCols2 >= p.w2;
-    store1x = x < p.w1 && (lane < cols || lastTile);
-  } else {
-    yb = band * p.band;
-    ye = min(yb + p.band, p.h1);
-    yStoreEnd = ye;
-    store1x = x < p.w1 && lane < cols;
-  }
-  const uint32_t X = x0 / 2 + (lane >> 1);  // level-(L+2) column of an even lane
-  const bool store2x = LEVELS == 2 && (lane & 1) == 0 && lane < 2 * kCols2 && X < p.w2;
-  const Axis3 ax2 = axis3(p.w2), ay2 = axis3(p.h2);
-  const Weights3 wX = weightsAt(ax2, min(X, p.w2 - 1));
-
-  // Level-L rows: lane texels at colA / colA + dB of row r.  Rows are read
-  // only while their level-(L+1) row is inside the band, so no row index
-  // leaves the level (for y < ye: 2y + 2 <= h0 - 1 with three taps, 2y + 1
-  // <= h0 - 1 with two).
-  const uint32_t dB = uint32_t(colB - colA);  // 4, or 0 where column 2x+1 is clamped
-  const uint64_t pitch = p.srcPitch;
-  auto ldGroup = [&](uint32_t yg, uint32_t (&raw)[kGroupRows][4]) {
-    const uint8_t* row = colA + uint64_t(TY0 ? 2 * yg + 1 : 2 * yg) * pitch;
-#pragma unroll
-    for (uint32_t j = 0; j < kGroupRows; ++j) {
-      if (yg + j < ye) {
-        raw[j][0] = ldTexel(row);
-        raw[j][1] = ldTexel(row + dB);
-        raw[j][2] = ldTexel(row + pitch);
-        raw[j][3] = ldTexel(row + pitch + dB);
-      }
-      row += 2 * pitch;
-    }
-  };
-
-  float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;  // three taps: level-L row 2y
-  if (TY0) {
-    const uint8_t* row = colA + uint64_t(2 * yb) * pitch;
-    pa = decodeAligned(ldTexel(row), L);
-    pb = decodeAligned(ldTexel(row + dB), L);
-  }
-  float4 h0v = make_float4(0.f, 0.f, 0.f, 0.f), h1v = h0v;  // level-(L+1) rows 2Y, 2Y+1
-
-  auto process = [&](uint32_t yg, const uint32_t (&raw)[kGroupRows][4]) {
-#pragma unroll
-    for (uint32_t j = 0; j < kGroupRows; ++j) {
-      const uint32_t y = yg + j;
-      if (y >= ye) break;
-      const float4 r1a = decodeAligned(raw[j][0], L), r1b = decodeAligned(raw[j][1], L);
-      const float4 r2a = decodeAligned(raw[j][2], L), r2b = decodeAligned(raw[j][3], L);
-      float4 va, vb;
-      if (TY0) {
-        const Weights3 wy = weightsAt(ay1, y);
-        va = reduce3p(wy, pa, r1a, r2a);
-        vb = reduce3p(wy, pb, r1b, r2b);
-        pa = r2a;
-        pb = r2b;
-      } else {
-        va = reduce2p(r1a, r2a);
-        vb = reduce2p(r1b, r2b);
-      }
-      float4 l1;
-      if (TX0)
-        l1 = reduce3p(wx, va, vb, shflDown(va, 1));
-      else
-        l1 = reduce2p(va, vb);
-      if (store1x && y < yStoreEnd)
-        *reinterpret_cast<uint32_t*>(p.dst1 + uint64_t(y) * p.pitch1 + uint64_t(x) * 4) = encodeTexel(l1, L);
-      if (LEVELS == 2) {
-        const uint32_t jj = y - yb;
-        bool emit = false;
-        uint32_t Y = 0;
-        float4 v2 = l1;
-        if (TY1) {
-          if (jj == 0) {
-            h0v = l1;
-          } else if (jj & 1) {
-            h1v = l1;
-          } else {
-            Y = (y - 2) >> 1;
-            v2 = reduce3p(weightsAt(ay2, Y), h0v, h1v, l1);
-            h0v = l1;
-            emit = true;
-          }
-        } else {
-          if ((jj & 1) == 0) {
-            h0v = l1;
-          } else {
-            Y = (y - 1) >> 1;
-            v2 = reduce2p(h0v, l1);
-            emit = true;
-          }
-        }
-        if (emit) {
-          const float4 n1 = shflDown(v2, 1);
-          const float4 o = TX1 ? reduce3p(wX, v2, n1, shflDown(v2, 2)) : reduce2p(v2, n1);
-          if (store2x)
-            *reinterpret_cast<uint32_t*>(p.dst2 + uint64_t(Y) * p.pitch2 + uint64_t(X) * 4) = encodeTexel(o, L);
-        }
-      }
-    }
-  };
-
-  // two row buffers in turn: the next group's rows load while this one reduces
-  uint32_t bufA[kGroupRows][4], bufB[kGroupRows][4];
-  ldGroup(yb, bufA);
-  for (uint32_t yg = yb;;) {
-    if (yg + kGroupRows < ye) ldGroup(yg + kGroupRows, bufB);
-    process(yg, bufA);
-    yg += kGroupRows;
-    if (yg >= ye) break;
-    if (yg + kGroupRows < ye) ldGroup(yg + kGroupRows, bufA);
-    process(yg, bufB);
-    yg += kGroupRows;
-    if (yg >= ye) break;
-  }
-}
-
-__device__ __forceinline__ uint32_t ldAcquire(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-// Grid barrier between stages (all CTAs are resident: cooperative launch).
-// Thread 0 of each CTA arrives on the counter after a release fence; the last
-// arrival resets the counter and publishes generation `gen + 1`; the others
-// poll the generation with nanosleep backoff, at most kWaitLimit times.
-// Returns false (after setting the error flag) if the wait gave up.
 __device__ __forceinline__ bool gridBarrier(const ChainParams& p, uint32_t& gen, uint32_t* okFlag) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t ok = 1;
-    const uint32_t next = gen + 1;
-    __threadfence();
-    if (atomicAdd(p.barrierCount, 1u) == gridDim.x - 1) {
-      atomicExch(p.barrierCount, 0u);
-      __threadfence();
-      atomicExch(p.barrierGen, next);
-    } else {
-      uint32_t it = 0;
-      while (ldAcquire(p.barrierGen) != next) {
-        if (++it >= kWaitLimit) {
-          atomicExch(p.errorFlag, 1u);
-          ok = 0;
-          break;
-        }
-        __nanosleep(256);
-      }
-    }
-    __threadfence();
-    *okFlag = ok;
-  }
-  __syncthreads();
-  ++gen;
-  return *okFlag != 0;
+  return gridBarrierWait(p.barrierCount, p.barrierGen, p.errorFlag, gen, okFlag);
 }
 
 __device__ __forceinline__ void runStage(const Stage& st, uint32_t lane, uint32_t warpId, uint32_t warps, const Lut& L) {
@@ -330,17 +45,12 @@ __device__ __forceinline__ void runStage(const Stage& st, uint32_t lane, uint32_
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const __grid_constant__ ChainParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint32_t okFlag;
-  const uint32_t base = smemAddr(smem);
-  const uint32_t decOff = (0x10000u - (base & 0xFFFFu)) & 0xFFFFu;
-  const uint32_t thrOff = decOff >= kLutThrBytes ? 0u : decOff + kLutDecodeBytes;
-  fillLut(reinterpret_cast<float*>(smem + decOff), reinterpret_cast<float*>(smem + thrOff), threadIdx.x, kThreads);
+  const Lut L = fillAlignedLut(smem, threadIdx.x, kThreads);
   uint32_t gen = 0;
   if (threadIdx.x == 0 && p.stageCount > 1) gen = ldAcquire(p.barrierGen);  // before this CTA's first arrival
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warpId = blockIdx.x * kWarps + (threadIdx.x >> 5), warps = gridDim.x * kWarps;
-  Lut L = makeLutAt(base + decOff, base + thrOff, lane);
-  L.laneWord |= (base + decOff) & 0xFFFF0000u;  // table bytes 2-3 for decodeAligned
 #pragma unroll 1
   for (uint32_t s = 0; s < p.stageCount; ++s) {
     runStage(p.st[s], lane, warpId, warps, L);
@@ -382,37 +92,12 @@ cudaError_t deviceState(int* sms, int* ctasPerSm) {
 }
 
 void makeStage(const DispatchParams& p, uint64_t warpsResident, Stage* g) {
-  *g = Stage{};
-  g->src = p.lv[0].ptr;
-  g->srcPitch = p.lv[0].pitch;
-  g->w0 = p.lv[0].w;
-  g->h0 = p.lv[0].h;
-  g->dst1 = p.lv[1].ptr;
-  g->pitch1 = p.lv[1].pitch;
-  g->w1 = p.lv[1].w;
-  g->h1 = p.lv[1].h;
-  const bool two = p.levelCount == 2;
-  if (two) {
-    g->dst2 = p.lv[2].ptr;
-    g->pitch2 = p.lv[2].pitch;
-    g->w2 = p.lv[2].w;
-    g->h2 = p.lv[2].h;
-  } else {
-    g->w2 = g->h2 = 1;
-  }
-  const bool tx0 = kernelSize(g->w0) == 3, ty0 = kernelSize(g->h0) == 3;
-  const bool tx1 = two && kernelSize(g->w1) == 3, ty1 = two && kernelSize(g->h1) == 3;
-  g->variant = two ? ((tx0 ? 8u : 0u) | (ty0 ? 4u : 0u) | (tx1 ? 2u : 0u) | (ty1 ? 1u : 0u))
-                   : 16u + (tx0 ? 2u : 0u) + (ty0 ? 1u : 0u);
+  stageGeometry(p, g);
   // Bands: about one strip per resident warp (a band's warp walks its rows
-  // serially), but at least 4 rows of the last level once the level is big
-  // enough to keep every warp busy.
-  const uint32_t lastW = two ? g->w2 : g->w1, lastH = two ? g->h2 : g->h1;
-  g->tilesX = (lastW + (two ? kCols2 : kCols1) - 1) / (two ? kCols2 : kCols1);
-  uint64_t band = (uint64_t(g->tilesX) * lastH + warpsResident - 1) / warpsResident;
-  band = std::max<uint64_t>(1, std::min<uint64_t>(band, lastH));
-  g->band = uint32_t(band);
-  g->bands = uint32_t((lastH + band - 1) / band);
+  // serially).
+  const uint32_t lastH = g->variant < 16 ? g->h2 : g->h1;
+  setStageBand(g, uint32_t(std::min<uint64_t>((uint64_t(g->tilesX) * lastH + warpsResident - 1) / warpsResident,
+                                               lastH)));
 }
 
 }  // namespace

@@ -246,3 +246,70 @@ def generate(chain: MipChain, stream: Optional[int] = None, mip_levels: int = 0,
     N.check(lib.nvproPyramidGenerate(cmd.handle, stream, pipelines.struct, ctypes.byref(img),
                                      mip_levels or chain.levels), "nvproPyramidGenerate")
     return cmd.launch_count
+
+
+class Batch:
+    """Many sRGBA8 chains generated by one persistent launch
+    (nvproPyramidCreateBatch / BatchBuild / BatchLaunch)."""
+
+    def __init__(self, flags: int = 0, preset: int = N.PRESET_SRGBA8):
+        self._lib = N.load()
+        self._h = ctypes.c_void_p()
+        N.check(self._lib.nvproPyramidCreateBatch(preset, flags, ctypes.byref(self._h)), "create batch")
+        self._images = None
+
+    def build(self, chains: Sequence["MipChain"], stream: Optional[int] = None, mip_levels: int = 0) -> None:
+        import torch
+        if stream is None:
+            dev = chains[0].storage.device if chains else torch.device("cuda")
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        arr = (N.NvproPyramidImage * max(len(chains), 1))()
+        for i, c in enumerate(chains):
+            arr[i] = c.image()
+        self._images = arr  # the library copies them; kept for inspection
+        N.check(self._lib.nvproPyramidBatchBuild(self._h, stream, arr, len(chains), mip_levels), "batch build")
+
+    def launch(self, stream: Optional[int] = None) -> None:
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream().cuda_stream
+        N.check(self._lib.nvproPyramidBatchLaunch(self._h, stream), "batch launch")
+
+    def info(self) -> dict:
+        inf = N.NvproPyramidBatchInfo()
+        N.check(self._lib.nvproPyramidBatchGetInfo(self._h, ctypes.byref(inf)), "batch info")
+        return {name: getattr(inf, name) for name, _ in N.NvproPyramidBatchInfo._fields_ if name != "reserved"}
+
+    def device_status(self) -> None:
+        N.check(self._lib.nvproPyramidBatchDeviceStatus(self._h), "batch device status")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h.value:
+            self._lib.nvproPyramidDestroyBatch(self._h)
+            self._h.value = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pack_chains(sizes: Sequence[tuple], device="cuda", align: int = 256):
+    """MipChains (sRGBA8) of the given (w, h) sizes in one device buffer, each
+    starting on an `align`-byte boundary.  Returns (storage, chains)."""
+    import torch
+    offs, total = [], 0
+    for w, h in sizes:
+        offs.append(total)
+        total += (packed_offsets(w, h, full_level_count(w, h), 4)[-1] + align - 1) // align * align
+    storage = torch.empty(max(total, 1), dtype=torch.uint8, device=device)
+    chains = []
+    for (w, h), o in zip(sizes, offs):
+        n = packed_offsets(w, h, full_level_count(w, h), 4)[-1]
+        chains.append(MipChain(w, h, N.PRESET_SRGBA8, device=device, storage=storage[o:o + n]))
+    return storage, chains
