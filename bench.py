@@ -197,6 +197,39 @@ def bench_config(w, h, dev, stream, flush, steps):
     return out
 
 
+def bench_batch(dev, stream, flush, steps):
+    """256 sRGBA8 images (sides log-uniform in [17, 4096], aspect in [1/4, 4],
+    seed 2024) in one buffer: one batch launch (autotuned, CUDA graph) against
+    256 per-image nvproPyramidGenerate calls, both device-timed, L2 flushed."""
+    import torch
+    import vk_compute_mipmaps_gb300 as V
+    from vk_compute_mipmaps_gb300.workloads import batch_sizes, chain_bytes
+    peak, _ = measured_peak()
+    sizes = batch_sizes(256)
+    storage, chains = V.pack_chains(sizes, device=dev)
+    g = torch.Generator(device=dev).manual_seed(2024)
+    storage.copy_(torch.randint(0, 256, (storage.numel(),), generator=g, device=dev, dtype=torch.uint8))
+    nbytes = sum(chain_bytes(w, h) for w, h in sizes)
+    with torch.cuda.stream(stream):
+        batch = V.Batch(V.BATCH_AUTOTUNE | V.BATCH_GRAPH)
+        batch.build(chains, stream=stream.cuda_stream)
+        tb = time_loop(lambda: batch.launch(stream.cuda_stream), stream, steps, 3, flush=flush)
+        tp = time_loop(lambda: [V.generate(c, stream=stream.cuda_stream) for c in chains], stream,
+                       max(3, steps // 4), 3, flush=flush)
+    b_us, p_us = statistics.median(tb) * 1e3, statistics.median(tp) * 1e3
+    info = batch.info()
+    batch.close()
+    del storage, chains
+    torch.cuda.empty_cache()
+    return {"images": len(sizes), "batch_us": round(b_us, 1), "plain_us": round(p_us, 1),
+            "batch_images_per_s": round(len(sizes) / (b_us * 1e-6), 1),
+            "plain_images_per_s": round(len(sizes) / (p_us * 1e-6), 1),
+            "speedup_vs_plain": round(p_us / b_us, 3), "algorithmic_bytes": nbytes,
+            "batch_frac_of_hbm_peak": round(nbytes / (b_us * 1e-6) / 1e9 / peak, 4),
+            "phases": info["phaseCount"], "jobs": info["jobCount"], "strip_band": info["stripBand"],
+            "launches_per_batch": 1}
+
+
 def bench_float_adjoint(dev, stream, flush, steps):
     """Linear float pyramids: forward (levels 1..) and adjoint (base gradient
     from upstream gradients of levels 1..) through the torch.autograd.Function
@@ -341,6 +374,7 @@ def run_ours(args, rank, world):
             torch.cuda.empty_cache()
             for cw, ch in CONFIGS:
                 extra[f"{cw}x{ch}"] = bench_config(cw, ch, dev, stream, flush, max(10, min(args.steps, 100)))
+            extra["batch_256"] = bench_batch(dev, stream, flush, max(5, min(args.steps, 20)))
             extra["float_adjoint"] = bench_float_adjoint(dev, stream, flush, max(5, min(args.steps, 20)))
             del flush
         if not args.no_cpu:
