@@ -32,6 +32,7 @@ constexpr uint32_t kCols2 = 15;     // level-(L+2) columns per strip (two levels
 constexpr uint32_t kCols1 = 31;     // level-(L+1) columns per strip (one level)
 constexpr uint32_t kGroupRows = 4;  // level-(L+1) rows whose level-L rows load together
 constexpr uint32_t kWaitLimit = 1u << 22;  // grid barrier polls (with backoff: about a second)
+constexpr uint32_t kTightPolls = 512;      // polls before the backoff starts
 
 // The replicated sRGB tables with the decode table at a 64 KiB boundary of
 // the shared window (decodeAligned): the threshold table below it if it fits
@@ -55,10 +56,12 @@ struct Stage {
 };
 
 // REDUCE / REDUCE2 (srgba8_mipmap_preamble.glsl:24-38), equal to reduce3() /
-// reduce2(): products on packed pairs (__fmul2_rn), sums with __fadd_rn.  The
-// sums must stay scalar: __fadd_rn is never merged into a multiply-add, while
-// packed adds next to packed multiplies were seen fused (a fused
-// w0*v0 + w1*v1 changes encoded bytes).
+// reduce2(): products on packed pairs (__fmul2_rn).  The sums of REDUCE must
+// stay scalar: __fadd_rn is never merged into a multiply-add, while packed
+// adds next to packed multiplies were seen fused (a fused w0*v0 + w1*v1
+// changes encoded bytes).  REDUCE2's add may be packed: its operands are
+// decoded values, sums, or exact halvings (0.5 * x), so a fused and an
+// unfused result are the same.
 __device__ __forceinline__ float4 mul4p(float s, float4 a) {
   const float2 lo = __fmul2_rn(make_float2(s, s), make_float2(a.x, a.y));
   const float2 hi = __fmul2_rn(make_float2(s, s), make_float2(a.z, a.w));
@@ -67,7 +70,7 @@ __device__ __forceinline__ float4 mul4p(float s, float4 a) {
 __device__ __forceinline__ float4 reduce3p(const Weights3& w, float4 v0, float4 v1, float4 v2) {
   return f4add(f4add(mul4p(w.w0, v0), mul4p(w.w1, v1)), mul4p(w.w2, v2));
 }
-__device__ __forceinline__ float4 reduce2p(float4 v0, float4 v1) { return mul4p(0.5f, f4add(v0, v1)); }
+__device__ __forceinline__ float4 reduce2p(float4 v0, float4 v1) { return mul4p(0.5f, add4p(v0, v1)); }
 
 // weights3(n, i) with the reciprocal 1 / (2n + 1) computed once per level.
 struct Axis3 {
@@ -93,6 +96,14 @@ __device__ __forceinline__ uint32_t ldTexel(const uint8_t* p) {
   uint32_t v;
   asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p));
   return v;
+}
+
+// Store `v` to `p` if `pred`: a predicated st.global, so the value (an
+// encode every lane computes anyway) is not moved into a divergent branch.
+__device__ __forceinline__ void storeIf(bool pred, uint8_t* p, uint32_t v) {
+  asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n @q st.global.u32 [%0], %1;\n}\n" ::"l"(p), "r"(v),
+               "r"(uint32_t(pred))
+               : "memory");
 }
 
 // decodeTexel for a decode table at a 64 KiB-aligned shared address: the
@@ -209,8 +220,7 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
         l1 = reduce3p(wx, va, vb, shflDown(va, 1));
       else
         l1 = reduce2p(va, vb);
-      if (store1x && y < yStoreEnd)
-        *reinterpret_cast<uint32_t*>(p.dst1 + uint64_t(y) * p.pitch1 + uint64_t(x) * 4) = encodeTexel(l1, L);
+      storeIf(store1x && y < yStoreEnd, p.dst1 + uint64_t(y) * p.pitch1 + uint64_t(x) * 4, encodeTexel(l1, L));
       if (LEVELS == 2) {
         const uint32_t jj = y - yb;
         bool emit = false;
@@ -239,8 +249,7 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
         if (emit) {
           const float4 n1 = shflDown(v2, 1);
           const float4 o = TX1 ? reduce3p(wX, v2, n1, shflDown(v2, 2)) : reduce2p(v2, n1);
-          if (store2x)
-            *reinterpret_cast<uint32_t*>(p.dst2 + uint64_t(Y) * p.pitch2 + uint64_t(X) * 4) = encodeTexel(o, L);
+          storeIf(store2x, p.dst2 + uint64_t(Y) * p.pitch2 + uint64_t(X) * 4, encodeTexel(o, L));
         }
       }
     }
@@ -284,6 +293,8 @@ __device__ __forceinline__ bool gridBarrierWait(uint32_t* count, uint32_t* genWo
       __threadfence();
       atomicExch(genWord, next);
     } else {
+      // a short tight spin (the last CTAs of a stage arrive close together),
+      // then polls with backoff
       uint32_t it = 0;
       while (ldAcquire(genWord) != next) {
         if (++it >= kWaitLimit) {
@@ -291,7 +302,7 @@ __device__ __forceinline__ bool gridBarrierWait(uint32_t* count, uint32_t* genWo
           ok = 0;
           break;
         }
-        __nanosleep(256);
+        if (it > kTightPolls) __nanosleep(256);
       }
     }
     __threadfence();
@@ -337,6 +348,24 @@ inline void setStageBand(Stage* g, uint32_t band) {
   band = band < 1 ? 1 : (band > lastH ? lastH : band);
   g->band = band;
   g->bands = (lastH + band - 1) / band;
+}
+
+// The last CTA to arrive returns true (the others false and may exit): a
+// hand-off without waiting.  Writes of every CTA before its arrival are
+// visible to the last one after (release / acquire fences around the count).
+__device__ __forceinline__ bool lastCtaArrives(uint32_t* count, uint32_t* flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const bool last = atomicAdd(count, 1u) == gridDim.x - 1;
+    if (last) {
+      atomicExch(count, 0u);
+      __threadfence();
+    }
+    *flag = last ? 1u : 0u;
+  }
+  __syncthreads();
+  return *flag != 0;
 }
 
 // Fill the aligned tables in `smem` (kAlignedLutSmemBytes of dynamic shared

@@ -35,7 +35,8 @@ constexpr uint32_t kWarps = 16;
 constexpr uint32_t kThreads = 32 * kWarps;
 constexpr uint32_t kRegion = 64;  // fast units: 64x64 texels of level L
 constexpr uint32_t kTopBytes = kMaxDispatchLevels * 32 * 16;  // per warp: fast-region rows kept per level
-constexpr uint32_t kSmemBytes = kAlignedLutSmemBytes + kWarps * kTopBytes;
+constexpr uint32_t kJobIndexMax = 1024;  // jobs of a phase whose first units are searched in shared memory
+constexpr uint32_t kSmemBytes = kAlignedLutSmemBytes + kWarps * kTopBytes + kJobIndexMax * 4;
 static_assert(kSmemBytes + 1024 <= 232448, "exceeds the shared memory of a CTA");
 constexpr uint32_t kFastGroupRows = 2;  // level-(L+1) rows of a fast region whose level-L rows load together
 
@@ -236,9 +237,15 @@ __global__ void __launch_bounds__(kThreads, 1) batchKernel(const __grid_constant
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31;
   float4* const top = reinterpret_cast<float4*>(smem + kAlignedLutSmemBytes + (threadIdx.x >> 5) * kTopBytes);
+  // first unit of each job of the current phase (the unit -> job search)
+  uint32_t* const jobStart = reinterpret_cast<uint32_t*>(smem + kAlignedLutSmemBytes + kWarps * kTopBytes);
 #pragma unroll 1
   for (uint32_t k = 0; k < p.phaseCount; ++k) {
     const uint32_t jb = p.phaseJobBegin[k], je = p.phaseJobBegin[k + 1], units = p.phaseUnits[k];
+    const bool inSmem = je - jb <= kJobIndexMax;
+    if (inSmem)
+      for (uint32_t j = threadIdx.x; j < je - jb; j += kThreads) jobStart[j] = p.jobs[jb + j].unitBegin;
+    __syncthreads();
     for (;;) {
       uint32_t u = 0;
       if (lane == 0) u = atomicAdd(p.unitCounters + k, 1u);
@@ -247,7 +254,7 @@ __global__ void __launch_bounds__(kThreads, 1) batchKernel(const __grid_constant
       uint32_t lo = jb, hi = je - 1;  // the last job of the phase with unitBegin <= u
       while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
-        if (p.jobs[mid].unitBegin <= u) lo = mid;
+        if ((inSmem ? jobStart[mid - jb] : p.jobs[mid].unitBegin) <= u) lo = mid;
         else hi = mid - 1;
       }
       const BatchJob& J = p.jobs[lo];

@@ -28,6 +28,7 @@ static_assert(kCtasPerSm * (kSmemBytes + 1024u) <= 228u * 1024u, "the CTAs of an
 struct ChainParams {
   Stage st[kMaxStages];
   uint32_t stageCount;
+  uint32_t tailFrom;       // stages from here on are small: one CTA runs them
   uint32_t* barrierCount;  // CTAs arrived at the current barrier (self-resetting)
   uint32_t* barrierGen;    // barrier generation (only ever incremented)
   uint32_t* errorFlag;     // set to 1 if a bounded wait gave up
@@ -51,10 +52,19 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warpId = blockIdx.x * kWarps + (threadIdx.x >> 5), warps = gridDim.x * kWarps;
+  const uint32_t localWarp = threadIdx.x >> 5;
 #pragma unroll 1
   for (uint32_t s = 0; s < p.stageCount; ++s) {
-    runStage(p.st[s], lane, warpId, warps, L);
-    if (s + 1 < p.stageCount && !gridBarrier(p, gen, &okFlag)) return;
+    const bool alone = s >= p.tailFrom;  // a small stage: this CTA alone
+    runStage(p.st[s], lane, alone ? localWarp : warpId, alone ? kWarps : warps, L);
+    if (s + 1 == p.stageCount) break;
+    if (s + 1 < p.tailFrom) {
+      if (!gridBarrier(p, gen, &okFlag)) return;
+    } else if (s + 1 == p.tailFrom) {
+      if (!lastCtaArrives(p.barrierCount, &okFlag)) return;  // the others are done
+    } else {
+      __syncthreads();  // the small stages: one CTA, block-level order
+    }
   }
 }
 
@@ -129,13 +139,20 @@ cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStre
     makeStage(p[i], uint64_t(ctas) * kWarps, &cp.st[i]);
     maxUnits = std::max<uint64_t>(maxUnits, uint64_t(cp.st[i].tilesX) * cp.st[i].bands);
   }
+  // Stages whose input fits one 64x64 region go to one CTA after the last
+  // larger one (a grid barrier costs more than their work); a chain of only
+  // such stages is one CTA from the start.
+  cp.tailFrom = count;
+  while (cp.tailFrom > 0 && p[cp.tailFrom - 1].lv[0].w <= 64 && p[cp.tailFrom - 1].lv[0].h <= 64) --cp.tailFrom;
+  for (uint32_t i = cp.tailFrom; i < count; ++i) makeStage(p[i], kWarps, &cp.st[i]);  // bands for one CTA
   if (count > 1) {
     cp.barrierCount = scratch.counters + kCounterBarrier;
     cp.barrierGen = scratch.counters + kCounterBarrierGen;
     cp.errorFlag = scratch.counters + kCounterError;
   }
-  // a single stage needs no more CTAs than its strips fill
-  const uint32_t grid = count > 1 ? ctas : uint32_t(std::min<uint64_t>((maxUnits + kWarps - 1) / kWarps, ctas));
+  // a single stage needs no more CTAs than its strips fill; small stages only: one
+  uint32_t grid = count > 1 ? ctas : uint32_t(std::min<uint64_t>((maxUnits + kWarps - 1) / kWarps, ctas));
+  if (cp.tailFrom == 0) grid = 1;
   void* args[] = {&cp};
   e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(generalChainKernel), dim3(grid), dim3(kThreads),
                                   args, kSmemBytes, stream);
