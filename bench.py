@@ -177,8 +177,13 @@ def time_loop(fn, stream, steps, warmup, flush=None):
     return [s.elapsed_time(e) for s, e in times]
 
 
-def bench_config(w, h, dev, stream, flush, steps):
+def bench_config(w, h, dev, stream, flush, steps, content="random"):
     chain = make_chain(w, h, dev)
+    if content == "smooth":
+        import torch
+        from vk_compute_mipmaps_gb300.workloads import smooth_field
+        base = torch.from_numpy(smooth_field(w, h, seed=w * 31 + h).reshape(-1))
+        chain.storage[:chain.offsets[1]].copy_(base)
     run = Runner(chain, stream)
     with __import__("torch").cuda.stream(stream):
         cold = time_loop(run, stream, steps, 3, flush=flush)
@@ -230,39 +235,121 @@ def bench_batch(dev, stream, flush, steps):
             "launches_per_batch": 1}
 
 
+def level_errors_fp64(levels, base):
+    """Per-level max |error| / max |FP64 value| of a power-of-two float
+    pyramid, against FP64 block means of the base (the fast pipeline's 2x2
+    box in exact arithmetic: level k is the mean of each 2^k x 2^k block)."""
+    import torch
+    errs = []
+    b = base[0].double() if base.dim() == 4 else base.double()
+    H, W = b.shape[0], b.shape[1]
+    for k, lv in enumerate(levels, start=1):
+        s = 1 << k
+        hk, wk = max(H >> k, 1), max(W >> k, 1)
+        ref = torch.zeros((hk, wk, 4), dtype=torch.float64, device=b.device)
+        rows = max(1, (1 << 22) // (W * s))  # a few M texels of the base at a time
+        for r0 in range(0, hk, rows):
+            r1 = min(hk, r0 + rows)
+            blk = b[r0 * s:r1 * s].reshape(r1 - r0, s, wk, s, 4)
+            ref[r0:r1] = blk.mean(dim=(1, 3))
+        got = (lv[0] if lv.dim() == 4 else lv).double()
+        errs.append(float((got - ref).abs().max() / ref.abs().max()))
+        del ref
+    return errs
+
+
 def bench_float_adjoint(dev, stream, flush, steps):
-    """Linear float pyramids: forward (levels 1..) and adjoint (base gradient
-    from upstream gradients of levels 1..) through the torch.autograd.Function
-    helpers.  Algorithmic bytes: forward = base read + levels written;
-    adjoint = upstream gradients read + base gradient written."""
+    """Linear float pyramids (RGBA32F, RGBA16F storage with FP32 arithmetic).
+
+    * 8 x 2048^2 x 4 FP32, uniform [0, 1): forward, and forward + backward
+      through the torch.autograd.Function with N(0, 1) upstream gradients on
+      every level;
+    * 1023 x 777 x 4 FP32 (three-tap kernels on every level): forward + backward;
+    * 16384^2 x 4 FP32 and FP16, log-normal(0, 1): forward and the adjoint
+      with N(0, 1) gradients on all 15 levels, %HBM, and the forward's
+      per-level error against FP64.
+    Algorithmic bytes: forward = base read + levels written; adjoint =
+    upstream gradients read + base gradient written."""
     import torch
     from vk_compute_mipmaps_gb300 import autograd as A
     from vk_compute_mipmaps_gb300.pyramid import level_sizes
     peak, _ = measured_peak()
     out = {}
-    for name, B, S, dt in (("fp32_8x2048x2048", 8, 2048, torch.float32),
-                           ("fp32_16384x16384", 1, 16384, torch.float32),
-                           ("fp16_16384x16384", 1, 16384, torch.float16)):
-        g = torch.Generator(device=dev).manual_seed(11)
-        base = torch.rand((B, S, S, 4), generator=g, device=dev).to(dt)
-        sizes = level_sizes(S, S)
-        ups = [None] + [torch.randn((B, h, w, 4), generator=g, device=dev).to(dt) for w, h in sizes[1:]]
-        esz = base.element_size() * 4
-        base_bytes = B * S * S * esz
-        lvl_bytes = B * sum(w * h for w, h in sizes[1:]) * esz
+    g = torch.Generator(device=dev).manual_seed(11)
+
+    def fwd_bwd_autograd(B, H, W):
+        base = torch.rand((B, H, W, 4), generator=g, device=dev).requires_grad_(True)
+        ups = [torch.randn((B, h, w, 4), generator=g, device=dev) for w, h in level_sizes(W, H)]
+
+        def fwd():
+            with torch.no_grad():
+                A.pyramid(base)
+
+        def both_outputs():  # upstream gradients on the Function's outputs, levels 1..n-1
+            base.grad = None
+            torch.autograd.backward(A.pyramid(base), ups[1:])
+
+        def both_all():  # on every level 0..n-1: level 0 is an alias of the base (with_base)
+            base.grad = None
+            torch.autograd.backward(A.pyramid(base, with_base=True), ups)
+
+        # the same work through the C ABI directly (one strided call each way, no autograd engine)
+        det = base.detach()
+
+        def fwd_c():
+            A.forward_levels(det)
+
+        def both_c():
+            A.forward_levels(det)
+            A.adjoint([None] + ups[1:], (B, H, W, 4), torch.float32, dev)
+
         with torch.cuda.stream(stream):
-            fwd = time_loop(lambda: A.forward_levels(base), stream, steps, 3, flush=flush)
-            bwd = time_loop(lambda: A.adjoint(ups, tuple(base.shape), dt, dev), stream, steps, 3, flush=flush)
-            both = time_loop(lambda: (A.forward_levels(base), A.adjoint(ups, tuple(base.shape), dt, dev)),
-                             stream, steps, 3, flush=flush)
-        f_us, b_us, fb_us = (statistics.median(t) * 1e3 for t in (fwd, bwd, both))
-        fb = base_bytes + lvl_bytes
-        out[name] = {"forward_us": round(f_us, 2), "adjoint_us": round(b_us, 2), "fwd_plus_bwd_us": round(fb_us, 2),
-                     "fwd_plus_bwd_over_fwd": round(fb_us / f_us, 3),
-                     "forward_frac_of_hbm_peak": round(fb / (f_us * 1e-6) / 1e9 / peak, 4),
-                     "adjoint_frac_of_hbm_peak": round(fb / (b_us * 1e-6) / 1e9 / peak, 4),
-                     "algorithmic_bytes_each": fb}
-        del base, ups
+            tf = time_loop(fwd, stream, steps, 3, flush=flush)
+            to = time_loop(both_outputs, stream, steps, 3, flush=flush)
+            ta = time_loop(both_all, stream, steps, 3, flush=flush)
+            tfc = time_loop(fwd_c, stream, steps, 3, flush=flush)
+            tbc = time_loop(both_c, stream, steps, 3, flush=flush)
+        f_us, o_us, a_us = (statistics.median(t) * 1e3 for t in (tf, to, ta))
+        fc_us, bc_us = statistics.median(tfc) * 1e3, statistics.median(tbc) * 1e3
+        res = {"forward_us": round(f_us, 2),
+               "fwd_plus_bwd_us": round(o_us, 2), "fwd_plus_bwd_over_fwd": round(o_us / f_us, 3),
+               "fwd_plus_bwd_all_levels_us": round(a_us, 2),
+               "fwd_plus_bwd_all_levels_over_fwd": round(a_us / f_us, 3),
+               "c_abi_forward_us": round(fc_us, 2), "c_abi_fwd_plus_bwd_us": round(bc_us, 2),
+               "c_abi_fwd_plus_bwd_over_fwd": round(bc_us / fc_us, 3),
+               "path": "torch.autograd.Function (one strided launch per dispatch each way); c_abi_*: the "
+                       "same strided calls without the autograd engine",
+               "note": "all_levels adds N(0,1) on level 0: the backward then reads the level-0 gradient "
+                       "too, 1.75x the forward's bytes"}
+        return res
+
+    out["fp32_8x2048x2048"] = fwd_bwd_autograd(8, 2048, 2048)
+    out["fp32_1023x777"] = fwd_bwd_autograd(1, 777, 1023)
+
+    for name, dt in (("fp32_16384x16384", torch.float32), ("fp16_16384x16384", torch.float16)):
+        S = 16384
+        base = torch.empty((1, S, S, 4), device=dev).log_normal_(0.0, 1.0, generator=g).to(dt)
+        sizes = level_sizes(S, S)
+        ups = [torch.randn((1, h, w, 4), generator=g, device=dev).to(dt) for w, h in sizes]
+        esz = base.element_size() * 4
+        base_bytes = S * S * esz
+        lvl_bytes = sum(w * h for w, h in sizes[1:]) * esz
+        with torch.cuda.stream(stream):
+            tf = time_loop(lambda: A.forward_levels(base), stream, steps, 3, flush=flush)
+            tb = time_loop(lambda: A.adjoint(ups, tuple(base.shape), dt, dev), stream, steps, 3, flush=flush)
+        f_us, b_us = statistics.median(tf) * 1e3, statistics.median(tb) * 1e3
+        f_bytes = base_bytes + lvl_bytes
+        b_bytes = base_bytes + lvl_bytes + base_bytes  # all 15 upstream levels read, base gradient written
+        levels = A.forward_levels(base)
+        torch.cuda.synchronize()
+        errs = level_errors_fp64(levels, base)
+        out[name] = {"forward_us": round(f_us, 2), "adjoint_us": round(b_us, 2),
+                     "forward_frac_of_hbm_peak": round(f_bytes / (f_us * 1e-6) / 1e9 / peak, 4),
+                     "adjoint_frac_of_hbm_peak": round(b_bytes / (b_us * 1e-6) / 1e9 / peak, 4),
+                     "forward_algorithmic_bytes": f_bytes, "adjoint_algorithmic_bytes": b_bytes,
+                     "values": "log-normal(0, 1)",
+                     "forward_max_rel_err_vs_fp64_per_level": [float(f"{e:.3g}") for e in errs]}
+        del base, ups, levels
         torch.cuda.empty_cache()
     return out
 
@@ -373,7 +460,11 @@ def run_ours(args, rank, world):
             del chain
             torch.cuda.empty_cache()
             for cw, ch in CONFIGS:
-                extra[f"{cw}x{ch}"] = bench_config(cw, ch, dev, stream, flush, max(10, min(args.steps, 100)))
+                # 2048^2: uniform random bytes; the others: a smooth seeded field with radial alpha
+                content = "random" if (cw, ch) == (2048, 2048) else "smooth"
+                extra[f"{cw}x{ch}"] = bench_config(cw, ch, dev, stream, flush, max(10, min(args.steps, 100)),
+                                                   content)
+                extra[f"{cw}x{ch}"]["content"] = content
             extra["batch_256"] = bench_batch(dev, stream, flush, max(5, min(args.steps, 20)))
             extra["float_adjoint"] = bench_float_adjoint(dev, stream, flush, max(5, min(args.steps, 20)))
             del flush
@@ -452,6 +543,46 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_profile(spec: str, reps: int):
+    """Run one workload `reps` times on cuda:0 without timing (for profilers)."""
+    import torch
+    import vk_compute_mipmaps_gb300 as V
+    dev = torch.device("cuda:0")
+    if spec == "batch256":
+        from vk_compute_mipmaps_gb300.workloads import batch_sizes
+        storage, chains = V.pack_chains(batch_sizes(256), device=dev)
+        g = torch.Generator(device=dev).manual_seed(2024)
+        storage.copy_(torch.randint(0, 256, (storage.numel(),), generator=g, device=dev, dtype=torch.uint8))
+        batch = V.Batch(0)
+        batch.build(chains)
+        for _ in range(reps):
+            batch.launch()
+        torch.cuda.synchronize()
+        batch.device_status()
+    elif spec.startswith("chain:"):
+        parts = spec.split(":")
+        w, h = map(int, parts[1].lower().split("x"))
+        mips = int(parts[2]) if len(parts) > 2 else 0
+        chain = make_chain(w, h, dev)
+        for _ in range(reps):
+            V.generate(chain, mip_levels=mips)
+        torch.cuda.synchronize()
+    elif spec.startswith("adjoint:"):
+        from vk_compute_mipmaps_gb300 import autograd as A
+        from vk_compute_mipmaps_gb300.pyramid import level_sizes
+        _, size, dtype = spec.split(":")
+        w, h = map(int, size.lower().split("x"))
+        dt = {"fp32": torch.float32, "fp16": torch.float16}[dtype]
+        g = torch.Generator(device=dev).manual_seed(11)
+        ups = [torch.randn((1, lh, lw, 4), generator=g, device=dev).to(dt) for lw, lh in level_sizes(w, h)]
+        for _ in range(reps):
+            A.adjoint(ups, (1, h, w, 4), dt, dev)
+        torch.cuda.synchronize()
+    else:
+        raise SystemExit(f"unknown --profile workload {spec!r}")
+    print(f"profile workload {spec}: {reps} runs done")
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -478,7 +609,13 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) measurement")
     ap.add_argument("--image", default="16384x16384", help="headline image WxH (smaller for profiling runs)")
+    ap.add_argument("--profile", default=None,
+                    help="run one workload --steps times and exit (for ncu): chain:WxH[:mipLevels], batch256 "
+                         "or adjoint:WxH:fp32|fp16")
     args = ap.parse_args(argv)
+    if args.profile:
+        run_profile(args.profile, args.steps)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

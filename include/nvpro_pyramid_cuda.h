@@ -274,6 +274,15 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerate(
     NvproPyramidCmd cmd, NvproPyramidStream stream, NvproPyramidPipelines pipelines,
     const NvproPyramidImage* pImage, uint32_t mipLevels);
 
+/* nvproPyramidGenerate for `count` images of the same size and layout (no
+ * reference counterpart): image i's level k is image->levels[k] + i *
+ * imageStrides[k] (bytes).  Every dispatch is one launch over all images (the
+ * portable kernels, image = grid z): for many float images, e.g. a
+ * [B, H, W, 4] tensor per level. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerateStrided(
+    NvproPyramidCmd cmd, NvproPyramidStream stream, NvproPyramidPipelines pipelines,
+    const NvproPyramidImage* image, const uint64_t* imageStrides, uint32_t count, uint32_t mipLevels);
+
 /* ------------------------------------------------------------------------ */
 /* Adjoint of the linear float pyramids.  No reference counterpart (the      */
 /* reference template admits float types, nvpro_pyramid.glsl:44-46, but has  */
@@ -297,6 +306,16 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidAdjoint(
     NvproPyramidStream stream, NvproPyramidPreset preset, const NvproPyramidImage* upstream,
     void* baseGrad, uint64_t baseGradPitch, uint32_t mipLevels, void* workspace,
     uint64_t workspaceBytes);
+
+/* nvproPyramidAdjoint for `count` images of the same size (no reference
+ * counterpart): image i's upstream level k is upstream->levels[k] + i *
+ * upstreamImageStrides[k] (bytes; may be NULL when count == 1), its base
+ * gradient baseGrad + i * baseGradImageStride; the workspace holds count times
+ * nvproPyramidAdjointWorkspaceBytes.  One launch per dispatch for all images. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidAdjointStrided(
+    NvproPyramidStream stream, NvproPyramidPreset preset, const NvproPyramidImage* upstream,
+    const uint64_t* upstreamImageStrides, void* baseGrad, uint64_t baseGradPitch, uint64_t baseGradImageStride,
+    uint32_t count, uint32_t mipLevels, void* workspace, uint64_t workspaceBytes);
 
 /* The whole default chain (both pipelines of `preset`, mipLevels == 0 for the
  * full chain) on `stream`, without allocating anything.  No counterpart in the

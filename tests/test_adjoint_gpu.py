@@ -152,3 +152,44 @@ def test_adjoint_2048_batch_closed_form(cuda):
         errs.append(abs(float(grad[b, y, x, c]) - ref))
         mags.append(abs(ref))
     assert max(errs) / max(mags) <= RTOL
+
+
+@pytest.mark.parametrize("dtype_name", ["float32", "float16"])
+@pytest.mark.parametrize("w,h", [(64, 48), (33, 20), (1, 5), (255, 256)])
+def test_strided_calls_equal_per_image_calls(cuda, dtype_name, w, h):
+    """nvproPyramidGenerateStrided / AdjointStrided over B images (one launch
+    per dispatch) write the bytes of B single-image calls."""
+    import torch
+
+    from vk_compute_mipmaps_gb300.autograd import adjoint, forward_levels
+    dt = getattr(torch, dtype_name)
+    B = 3
+    g = torch.Generator(device=cuda).manual_seed(w * h)
+    base = torch.rand((B, h, w, 4), generator=g, device=cuda).to(dt)
+    levels = forward_levels(base)
+    ups = [torch.randn((B, lh, lw, 4), generator=g, device=cuda).to(dt) for lw, lh in P.level_sizes(w, h)]
+    grad = adjoint(ups, (B, h, w, 4), dt, cuda)
+    for i in range(B):
+        one = forward_levels(base[i:i + 1].clone())
+        for a, b in zip(levels, one):
+            assert torch.equal(a[i], b[0])
+        gi = adjoint([u[i:i + 1].clone() for u in ups], (1, h, w, 4), dt, cuda)
+        assert torch.equal(grad[i], gi[0])
+
+
+def test_autograd_with_base_takes_level0_gradient(cuda):
+    """pyramid(base, with_base=True): the level-0 gradient enters the adjoint
+    (h_0 = g_0 + A^T h_1), the same as the direct call with g_0."""
+    import torch
+
+    from vk_compute_mipmaps_gb300.autograd import adjoint, pyramid
+    B, H, W = 2, 40, 24
+    g = torch.Generator(device=cuda).manual_seed(8)
+    base = torch.rand((B, H, W, 4), generator=g, device=cuda, requires_grad=True)
+    levels = pyramid(base, with_base=True)
+    assert len(levels) == P.full_level_count(W, H) and torch.equal(levels[0], base)
+    ups = [torch.randn(l.shape, generator=g, device=cuda) for l in levels]
+    torch.autograd.backward(levels, ups)
+    assert torch.equal(base.grad, adjoint(ups, tuple(base.shape), torch.float32, cuda))
+    ref = dense_adjoint([u[0].double().cpu().numpy() for u in ups], W, H)
+    assert rel_err(base.grad[0].double().cpu().numpy(), ref) <= RTOL

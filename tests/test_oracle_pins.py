@@ -21,6 +21,7 @@ import numpy as np
 import pytest
 
 import _oracle as O
+from vk_compute_mipmaps_gb300.workloads import smooth_field
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
@@ -139,23 +140,6 @@ def test_reference_fp32_formulas_within_one_code():
     mine = O.srgb_encode_array(xs).astype(int)
     ref = np.array([lib.orc_ref_srgb_from_linear(float(x)) for x in xs])
     assert np.abs(mine - ref).max() <= 1
-
-
-def smooth_field(w, h, seed, opaque):
-    """Sum of 8 random-phase sinusoids (wavelengths 8..512 px) + uniform +-16 noise; radial alpha."""
-    rng = np.random.default_rng(seed)
-    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
-    img = np.zeros((h, w, 4))
-    for c in range(3):
-        acc = np.zeros((h, w))
-        for _ in range(8):
-            lam = np.exp(rng.uniform(np.log(8), np.log(512)))
-            th = rng.uniform(0, 2 * np.pi)
-            acc += np.sin(2 * np.pi * (x * np.cos(th) + y * np.sin(th)) / lam + rng.uniform(0, 2 * np.pi))
-        img[..., c] = 128 + 14 * acc + rng.uniform(-16, 16, (h, w))
-    r = np.hypot(x - w / 2, y - h / 2) / max(np.hypot(w / 2, h / 2), 1)
-    img[..., 3] = 255 if opaque else 255 * (1 - r)
-    return np.clip(np.rint(img), 0, 255).astype(np.uint8)
 
 
 @pytest.mark.parametrize("w,h", [(256, 256), (255, 255), (254, 254), (192, 108), (257, 129)])

@@ -114,7 +114,7 @@ def test_general_one_level_bit_exact(cuda, w, h):
 
 @pytest.mark.parametrize("w,h", BIG)
 def test_srgba8_bit_exact_large(cuda, w, h):
-    from test_oracle_pins import smooth_field
+    from vk_compute_mipmaps_gb300.workloads import smooth_field
     base = smooth_field(w, h, 5, opaque=False)
     mips = P.full_level_count(w, h)
     want = None
@@ -134,6 +134,32 @@ def test_float_presets_bit_exact(cuda, preset, w, h):
     for flags in (0, N.CMD_PORTABLE_KERNELS):
         got, sched, _ = gpu_run(cuda, preset, base, flags)
         assert_same(got, oracle_bytes(preset, base, sched, mips), w, h, O.BPP[preset], mips, f"{preset} {w}x{h}")
+
+
+@pytest.mark.parametrize("w,h", [(64, 64), (193, 97), (2052, 36)])
+def test_srgba8_strided_equals_per_image(cuda, w, h):
+    """nvproPyramidGenerateStrided over B sRGBA8 images (portable kernels, one
+    launch per dispatch) writes the bytes of per-image nvproPyramidGenerate."""
+    import torch
+    B = 3
+    lib = N.load()
+    sizes = P.level_sizes(w, h)
+    g = torch.Generator(device=cuda).manual_seed(w + h)
+    lv = [torch.full((B, lh, lw, 4), SENTINEL, dtype=torch.uint8, device=cuda) for lw, lh in sizes]
+    lv[0].copy_(torch.randint(0, 256, lv[0].shape, generator=g, device=cuda, dtype=torch.uint8))
+    img = P.make_image([t.data_ptr() for t in lv], w, h)
+    strides = (ctypes.c_uint64 * N.MAX_LEVELS)(*[t[0].numel() for t in lv])
+    cmd, pipes = P.Cmd(), P.Pipelines(N.PRESET_SRGBA8)
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    N.check(lib.nvproPyramidGenerateStrided(cmd.handle, stream, pipes.struct, ctypes.addressof(img),
+                                            ctypes.addressof(strides), B, 0))
+    torch.cuda.synchronize()
+    for i in range(B):
+        got = np.concatenate([t[i].cpu().numpy().reshape(-1) for t in lv])
+        mips = len(sizes)
+        want = oracle_bytes(N.PRESET_SRGBA8, lv[0][i].cpu().numpy(), [tuple(s) for s in O.default_schedule(w, h)],
+                            mips)
+        assert_same(got, want, w, h, 4, mips, f"strided image {i} of {w}x{h}")
 
 
 def fast_variant(div, mx):

@@ -139,6 +139,11 @@ SIGNATURES = {
     "nvproPyramidAdjoint": (c_int, [c_void_p, c_int, POINTER(NvproPyramidImage), c_void_p, c_uint64, c_uint32,
                                     c_void_p, c_uint64]),
     "nvproPyramidGenerateNoAlloc": (c_int, [c_void_p, c_int, POINTER(NvproPyramidImage), c_uint32]),
+    # image / stride arrays by address (the autograd helpers pass numpy buffers)
+    "nvproPyramidGenerateStrided": (c_int, [c_void_p, c_void_p, NvproPyramidPipelines, c_void_p, c_void_p, c_uint32,
+                                            c_uint32]),
+    "nvproPyramidAdjointStrided": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_uint64, c_uint64,
+                                           c_uint32, c_uint32, c_void_p, c_uint64]),
     "nvproPyramidGenerate": (c_int, [c_void_p, c_void_p, NvproPyramidPipelines, POINTER(NvproPyramidImage),
                                      c_uint32]),
 }

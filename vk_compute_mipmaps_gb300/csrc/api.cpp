@@ -77,6 +77,9 @@ struct NvproPyramidCmd_T {
   std::vector<Record> records;
   uint32_t launches = 0;
   Scratch scratch{nullptr, 0};
+  // set by nvproPyramidGenerateStrided for the duration of one EndCmd
+  uint32_t batch = 1;
+  uint64_t imageStrides[NVPRO_PYRAMID_MAX_LEVELS] = {};
 };
 
 namespace {
@@ -113,6 +116,7 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "dispatch writes level %u but the image has %u levels",
                 L + n, img.levelCount);
   std::memset(out, 0, sizeof *out);
+  out->batch = 1;  // one image unless a strided call says otherwise
   out->preset = rec.info.preset;
   out->isFast = rec.info.isFastPipeline;
   out->inputLevel = L;
@@ -374,9 +378,13 @@ NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
   for (size_t i = 0; i < cmd->records.size(); ++i) {
     NvproPyramidResult r = makeParams(cmd->records[i], &params[i]);
     if (r != NVPRO_PYRAMID_SUCCESS) return r;
+    params[i].batch = cmd->batch;
+    for (uint32_t k = 0; k <= params[i].levelCount; ++k)
+      params[i].imageStride[k] = cmd->imageStrides[params[i].inputLevel + k];
   }
   const bool fuse = !(cmd->flags & NVPRO_PYRAMID_CMD_NO_FUSION);
-  const bool portableOnly = (cmd->flags & NVPRO_PYRAMID_CMD_PORTABLE_KERNELS) != 0;
+  // strided batches run on the portable kernels (one launch per dispatch, grid z = image)
+  const bool portableOnly = (cmd->flags & NVPRO_PYRAMID_CMD_PORTABLE_KERNELS) != 0 || cmd->batch > 1;
   size_t i = 0;
   while (i < params.size()) {
     const DispatchParams& p = params[i];
@@ -671,6 +679,19 @@ uint64_t nvproPyramidAdjointWorkspaceBytes(uint32_t width, uint32_t height, uint
 NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPreset preset,
                                        const NvproPyramidImage* upstream, void* baseGrad, uint64_t baseGradPitch,
                                        uint32_t mipLevels, void* workspace, uint64_t workspaceBytes) {
+  return nvproPyramidAdjointStrided(stream, preset, upstream, nullptr, baseGrad, baseGradPitch, 0, 1, mipLevels,
+                                    workspace, workspaceBytes);
+}
+
+NvproPyramidResult nvproPyramidAdjointStrided(NvproPyramidStream stream, NvproPyramidPreset preset,
+                                              const NvproPyramidImage* upstream, const uint64_t* upstreamImageStrides,
+                                              void* baseGrad, uint64_t baseGradPitch, uint64_t baseGradImageStride,
+                                              uint32_t count, uint32_t mipLevels, void* workspace,
+                                              uint64_t workspaceBytes) {
+  if (count == 0) return NVPRO_PYRAMID_SUCCESS;
+  if (count > 65535) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u images: at most 65535", count);
+  if (count > 1 && !upstreamImageStrides)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "upstreamImageStrides is NULL");
   if (preset != NVPRO_PYRAMID_PRESET_RGBA32F && preset != NVPRO_PYRAMID_PRESET_RGBA16F)
     return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "the adjoint exists for the linear float presets only");
   if (!upstream || !baseGrad) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "NULL upstream or baseGrad");
@@ -692,19 +713,31 @@ NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPr
         (reinterpret_cast<uintptr_t>(upstream->levels[k]) % bpp || pitch % bpp || pitch < uint64_t(levelDim(w, k)) * bpp))
       return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "upstream level %u pitch/alignment invalid", k);
   }
+  uint64_t stride[NVPRO_PYRAMID_MAX_LEVELS] = {};
+  for (uint32_t k = 0; k < mipLevels && count > 1; ++k) {
+    stride[k] = upstreamImageStrides[k];
+    if (stride[k] % bpp) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "image stride of level %u", k);
+  }
+  if (count > 1 && baseGradImageStride % bpp)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "baseGrad image stride is not a texel multiple");
   uint64_t wsOff[NVPRO_PYRAMID_MAX_LEVELS];
-  const uint64_t wsNeed = adjointWorkspaceLayout(w, h, mipLevels, wsOff);
+  const uint64_t wsImage = adjointWorkspaceLayout(w, h, mipLevels, wsOff);  // one image's share
+  const uint64_t wsNeed = wsImage * count;
   if (wsNeed > workspaceBytes || (wsNeed && (!workspace || reinterpret_cast<uintptr_t>(workspace) % 16)))
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "workspace of %llu bytes (16-byte aligned) needed, got %llu",
                 (unsigned long long)wsNeed, (unsigned long long)workspaceBytes);
   if (mipLevels == 1) {  // no levels above the base: the gradient is the upstream one
     const uint64_t rowBytes = uint64_t(w) * bpp;
     const uint64_t srcPitch = upstream->rowPitchBytes[0] ? upstream->rowPitchBytes[0] : rowBytes;
-    cudaError_t e = upstream->levels[0]
-                        ? cudaMemcpy2DAsync(baseGrad, baseGradPitch, upstream->levels[0], srcPitch, rowBytes, h,
-                                            cudaMemcpyDeviceToDevice, reinterpret_cast<cudaStream_t>(stream))
-                        : cudaMemset2DAsync(baseGrad, baseGradPitch, 0, rowBytes, h,
-                                            reinterpret_cast<cudaStream_t>(stream));
+    cudaError_t e = cudaSuccess;
+    for (uint32_t i = 0; i < count && e == cudaSuccess; ++i) {
+      uint8_t* dst = static_cast<uint8_t*>(baseGrad) + i * baseGradImageStride;
+      e = upstream->levels[0]
+              ? cudaMemcpy2DAsync(dst, baseGradPitch, static_cast<const uint8_t*>(upstream->levels[0]) + i * stride[0],
+                                  srcPitch, rowBytes, h, cudaMemcpyDeviceToDevice,
+                                  reinterpret_cast<cudaStream_t>(stream))
+              : cudaMemset2DAsync(dst, baseGradPitch, 0, rowBytes, h, reinterpret_cast<cudaStream_t>(stream));
+    }
     return e == cudaSuccess ? NVPRO_PYRAMID_SUCCESS : fail(NVPRO_PYRAMID_ERROR_CUDA, "%s", cudaGetErrorString(e));
   }
   const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -714,6 +747,7 @@ NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPr
   auto hPtr = [&](uint32_t k) { return k == 0 ? static_cast<uint8_t*>(baseGrad) : ws + wsOff[k]; };
   auto hPitch = [&](uint32_t k) { return k == 0 ? baseGradPitch : uint64_t(levelDim(w, k)) * 16; };
   auto hType = [&](uint32_t k) { return k == 0 ? gType : 0u; };
+  auto hImage = [&](uint32_t k) { return k == 0 ? baseGradImageStride : wsImage; };
   auto gPtr = [&](uint32_t k) { return static_cast<const uint8_t*>(upstream->levels[k]); };
   auto gPitch = [&](uint32_t k) {
     return upstream->rowPitchBytes[k] ? upstream->rowPitchBytes[k] : uint64_t(levelDim(w, k)) * bpp;
@@ -728,6 +762,7 @@ NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPr
     const uint8_t* srcTop = hi == top ? gPtr(top) : hPtr(hi);
     const uint64_t srcPitch = hi == top ? gPitch(top) : hPitch(hi);
     const uint32_t srcType = hi == top ? gType : 0u;
+    const uint64_t srcImage = hi == top ? stride[top] : wsImage;
     cudaError_t e;
     if (d.isFast) {
       AdjointChainParams p{};
@@ -745,12 +780,17 @@ NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPr
       p.out = hPtr(L);
       p.outPitch = hPitch(L);
       p.outType = hType(L);
+      p.batch = count;
+      for (uint32_t k = 0; k < d.count; ++k) p.gImage[k] = stride[L + k];
+      p.topImage = srcImage;
+      p.outImage = hImage(L);
       e = launchAdjointChain(p, s);
     } else {
       e = cudaSuccess;
       const uint8_t* hc = srcTop;
       uint64_t hcPitch = srcPitch;
       uint32_t hcType = srcType;
+      uint64_t hcImage = srcImage;
       for (int k = int(hi) - 1; k >= int(L) && e == cudaSuccess; --k) {
         AdjointLevelParams p{};
         p.fw = levelDim(w, k);
@@ -766,10 +806,15 @@ NvproPyramidResult nvproPyramidAdjoint(NvproPyramidStream stream, NvproPyramidPr
         p.out = hPtr(k);
         p.outPitch = hPitch(k);
         p.outType = hType(k);
+        p.batch = count;
+        p.gImage = stride[k];
+        p.hcImage = hcImage;
+        p.outImage = hImage(k);
         e = launchAdjointLevel(p, s);
         hc = hPtr(k);
         hcPitch = hPitch(k);
         hcType = hType(k);
+        hcImage = hImage(k);
       }
     }
     if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "adjoint launch failed: %s", cudaGetErrorString(e));
@@ -835,6 +880,29 @@ NvproPyramidResult nvproPyramidGenerate(NvproPyramidCmd cmd, NvproPyramidStream 
   nvproPyramidCmdBindImage(cmd, pImage);
   if (pImage) nvproCmdPyramidDispatch(cmd, pipelines, pImage->width, pImage->height, mipLevels);
   return nvproPyramidEndCmd(cmd);
+}
+
+NvproPyramidResult nvproPyramidGenerateStrided(NvproPyramidCmd cmd, NvproPyramidStream stream,
+                                               NvproPyramidPipelines pipelines, const NvproPyramidImage* pImage,
+                                               const uint64_t* imageStrides, uint32_t count, uint32_t mipLevels) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (count == 0) return NVPRO_PYRAMID_SUCCESS;
+  if (count > 65535) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u images: at most 65535", count);
+  if (count > 1 && !imageStrides) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "imageStrides is NULL");
+  if (count > 1 && pImage) {
+    const uint32_t bpp =
+        presetBytes(validPipeline(pipelines.generalPipeline) ? pipelines.generalPipeline->preset : 0);
+    for (uint32_t k = 0; k < pImage->levelCount && k < NVPRO_PYRAMID_MAX_LEVELS; ++k)
+      if (bpp && imageStrides[k] % bpp)
+        return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "image stride of level %u is not a texel multiple", k);
+  }
+  cmd->batch = count;
+  for (uint32_t k = 0; k < NVPRO_PYRAMID_MAX_LEVELS; ++k)
+    cmd->imageStrides[k] = count > 1 && pImage && k < pImage->levelCount ? imageStrides[k] : 0;
+  const NvproPyramidResult r = nvproPyramidGenerate(cmd, stream, pipelines, pImage, mipLevels);
+  cmd->batch = 1;
+  std::memset(cmd->imageStrides, 0, sizeof cmd->imageStrides);
+  return r;
 }
 
 }  // extern "C"

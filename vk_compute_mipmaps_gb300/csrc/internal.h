@@ -30,6 +30,10 @@ struct DispatchParams {
   uint32_t levelCount;  // n
   uint64_t groups;      // reference workgroups covered (gx if gy, gz > 0, else 0)
   LevelView lv[kMaxDispatchLevels + 1];
+  // Strided batches (portable kernels only): `batch` images, image i's level
+  // L+k at lv[k].ptr + i * imageStride[k].
+  uint32_t batch = 1;
+  uint64_t imageStride[kMaxDispatchLevels + 1] = {};
 };
 
 // Device scratch owned by a command object (allocated at creation).
@@ -67,6 +71,10 @@ struct AdjointChainParams {
   uint32_t outType;
   uint8_t* out;  // h of level L
   uint64_t outPitch;
+  // strided batches: image z at + z * stride (grid z = image)
+  uint32_t batch;
+  uint64_t gImage[kMaxDispatchLevels];
+  uint64_t topImage, outImage;
 };
 struct AdjointLevelParams {
   uint32_t fw, fh, cw, ch;  // fine level k, coarse level k+1
@@ -79,6 +87,8 @@ struct AdjointLevelParams {
   uint8_t* out;  // h of level k
   uint64_t outPitch;
   uint32_t outType;
+  uint32_t batch;  // strided batches: image z at + z * stride (grid z = image)
+  uint64_t gImage, hcImage, outImage;
 };
 // The general pipeline for sRGBA8 as streaming column strips
 // (kernels_general.cu): dispatches of 1 or 2 levels whose input level is at

@@ -59,9 +59,10 @@ struct View {
   }
 };
 
+// The view of image blockIdx.z of a level (image stride `image` bytes).
 template <bool F16>
-__device__ __forceinline__ View viewOf(const uint8_t* p, uint64_t pitch) {
-  if (p) return View{p, pitch, Grad<F16>::kBytes};
+__device__ __forceinline__ View viewOf(const uint8_t* p, uint64_t pitch, uint64_t image) {
+  if (p) return View{p + uint64_t(blockIdx.z) * image, pitch, Grad<F16>::kBytes};
   return View{reinterpret_cast<const uint8_t*>(g_zeroTexel), 0, 0};
 }
 
@@ -84,10 +85,12 @@ __global__ void __launch_bounds__(kThreads) adjointChainKernel(AdjointChainParam
   const uint32_t x = blockIdx.x * 32 + lane;
   if (x >= p.w) return;
   const uint32_t n = p.n;
-  const View top = viewOf<TF16>(p.top, p.topPitch);
+  const View top = viewOf<TF16>(p.top, p.topPitch, p.topImage);
   View g[kMaxDispatchLevels];
 #pragma unroll
-  for (uint32_t k = 0; k < kMaxDispatchLevels; ++k) g[k] = viewOf<GF16>(k < n ? p.g[k] : nullptr, p.gPitch[k]);
+  for (uint32_t k = 0; k < kMaxDispatchLevels; ++k)
+    g[k] = viewOf<GF16>(k < n ? p.g[k] : nullptr, p.gPitch[k], p.gImage[k]);
+  uint8_t* const out = p.out + uint64_t(blockIdx.z) * p.outImage;
   for (uint32_t y0 = (blockIdx.y * kWarps + warp) * R; y0 < p.h; y0 += gridDim.y * kWarps * R) {
     // every load of the strip first, then the arithmetic
     const float4 t = Grad<TF16>::load(top.at(x >> n, y0 >> n));
@@ -114,7 +117,7 @@ __global__ void __launch_bounds__(kThreads) adjointChainKernel(AdjointChainParam
     }
 #pragma unroll
     for (uint32_t j = 0; j < R; ++j)
-      Grad<OF16>::store(p.out + uint64_t(y0 + j) * p.outPitch + uint64_t(x) * Grad<OF16>::kBytes, cur[j]);
+      Grad<OF16>::store(out + uint64_t(y0 + j) * p.outPitch + uint64_t(x) * Grad<OF16>::kBytes, cur[j]);
   }
 }
 
@@ -166,8 +169,9 @@ __global__ void __launch_bounds__(kThreads) adjointLevelKernel(AdjointLevelParam
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t x = blockIdx.x * 32 + lane;
   if (x >= p.fw) return;
-  const View g = viewOf<GF16>(p.g, p.gPitch);
-  const View hc = viewOf<CF16>(p.hc, p.hcPitch);
+  const View g = viewOf<GF16>(p.g, p.gPitch, p.gImage);
+  const View hc = viewOf<CF16>(p.hc, p.hcPitch, p.hcImage);
+  uint8_t* const out = p.out + uint64_t(blockIdx.z) * p.outImage;
   const Parents px = axisParents(x, p.fw, p.cw);
   for (uint32_t y = blockIdx.y * kWarps + warp; y < p.fh; y += gridDim.y * kWarps) {
     const Parents py = axisParents(y, p.fh, p.ch);
@@ -189,22 +193,22 @@ __global__ void __launch_bounds__(kThreads) adjointLevelKernel(AdjointLevelParam
         t = addScaled(t, py.w[b], s);
       }
     }
-    Grad<OF16>::store(p.out + uint64_t(y) * p.outPitch + uint64_t(x) * Grad<OF16>::kBytes, f4add(gk, t));
+    Grad<OF16>::store(out + uint64_t(y) * p.outPitch + uint64_t(x) * Grad<OF16>::kBytes, f4add(gk, t));
   }
 }
 
 // 2D grid: one block column per 32 texel columns, enough block rows for
 // about 32 blocks per SM, each warp stepping over `rowsPerWarp`-row strips.
-dim3 gridFor(uint32_t w, uint32_t h, uint32_t rowsPerWarp) {
+dim3 gridFor(uint32_t w, uint32_t h, uint32_t rowsPerWarp, uint32_t batch) {
   const uint32_t gx = (w + 31) / 32;
   const uint32_t rowsNeeded = (h + kWarps * rowsPerWarp - 1) / (kWarps * rowsPerWarp);
-  const uint32_t target = (152u * 32u + gx - 1) / gx;
-  return dim3(gx, std::max(1u, std::min(rowsNeeded, target)));
+  const uint32_t target = (152u * 32u + gx * batch - 1) / (gx * batch);
+  return dim3(gx, std::max(1u, std::min(rowsNeeded, target)), batch);
 }
 
 template <uint32_t LR, bool GF16>
 void launchChain(const AdjointChainParams& p, cudaStream_t s) {
-  const dim3 grid = gridFor(p.w, p.h, 1u << LR);
+  const dim3 grid = gridFor(p.w, p.h, 1u << LR, p.batch);
   const uint32_t sel = (p.topType ? 2u : 0u) | (p.outType ? 1u : 0u);
   switch (sel) {
     case 0: adjointChainKernel<LR, GF16, false, false><<<grid, kThreads, 0, s>>>(p); break;
@@ -216,7 +220,7 @@ void launchChain(const AdjointChainParams& p, cudaStream_t s) {
 
 template <bool GF16>
 void launchLevel(const AdjointLevelParams& p, cudaStream_t s) {
-  const dim3 grid = gridFor(p.fw, p.fh, 1);
+  const dim3 grid = gridFor(p.fw, p.fh, 1, p.batch);
   const uint32_t sel = (p.hcType ? 2u : 0u) | (p.outType ? 1u : 0u);
   switch (sel) {
     case 0: adjointLevelKernel<GF16, false, false><<<grid, kThreads, 0, s>>>(p); break;

@@ -24,6 +24,13 @@ struct SmemTables {
   SrgbTablesSmem t;
 };
 
+// Level L+k of this CTA's image (blockIdx.z of a strided batch).
+__device__ __forceinline__ LevelView levelOf(const DispatchParams& p, uint32_t k) {
+  LevelView v = p.lv[k];
+  v.ptr += uint64_t(blockIdx.z) * p.imageStride[k];
+  return v;
+}
+
 template <uint32_t P>
 __device__ __forceinline__ TexelIO<P> makeIO(SrgbTablesSmem* t) {
   TexelIO<P> io;
@@ -52,7 +59,7 @@ __global__ void __launch_bounds__(kThreads) portableFastKernel(DispatchParams p)
   constexpr uint32_t B = TexelIO<P>::kBytes;
 
   const uint32_t n = p.levelCount;
-  const LevelView& src = p.lv[0];
+  const LevelView src = levelOf(p, 0);
   const uint32_t tilesX = src.w >> n, tilesY = src.h >> n;
   const uint32_t coverW = tilesX << n, coverH = tilesY << n;
   const uint32_t regionsX = (coverW + kRegion - 1) / kRegion;
@@ -66,6 +73,7 @@ __global__ void __launch_bounds__(kThreads) portableFastKernel(DispatchParams p)
   };
 
   // Level L+1 from global level L: LOAD_REDUCE4 (nvpro_pyramid.glsl:180-188).
+  const LevelView dst1 = levelOf(p, 1);
   uint32_t ew = rw / 2, eh = rh / 2;
   for (uint32_t i = threadIdx.x; i < ew * eh; i += kThreads) {
     const uint32_t x = i % ew, y = i / ew;
@@ -76,7 +84,7 @@ __global__ void __launch_bounds__(kThreads) portableFastKernel(DispatchParams p)
     const float4 v11 = io.load(texelAddr(src, sx + 1, sy + 1, B));
     const float4 v = reduce4(v00, v01, v10, v11);
     bufA[y * 32 + x] = v;
-    if (covered(sx, sy)) io.store(texelAddr(p.lv[1], x0 / 2 + x, y0 / 2 + y, B), v);
+    if (covered(sx, sy)) io.store(texelAddr(dst1, x0 / 2 + x, y0 / 2 + y, B), v);
   }
   __syncthreads();
 
@@ -94,7 +102,7 @@ __global__ void __launch_bounds__(kThreads) portableFastKernel(DispatchParams p)
       const float4 v = fastReduce(vert, tl, tr, bl, br);
       nxt[y * nStride + x] = v;
       if (covered(x0 + (x << k), y0 + (y << k)))
-        io.store(texelAddr(p.lv[k], (x0 >> k) + x, (y0 >> k) + y, B), v);
+        io.store(texelAddr(levelOf(p, k), (x0 >> k) + x, (y0 >> k) + y, B), v);
     }
     __syncthreads();
     float4* t = cur;
@@ -148,8 +156,8 @@ __global__ void __launch_bounds__(kThreads) portableGeneral1Kernel(DispatchParam
   }
   const TexelIO<P> io = makeIO<P>(&tabs);
   constexpr uint32_t B = TexelIO<P>::kBytes;
-  const LevelView& src = p.lv[0];
-  const LevelView& dst = p.lv[1];
+  const LevelView src = levelOf(p, 0);
+  const LevelView dst = levelOf(p, 1);
   const uint32_t kx = kernelSize(src.w), ky = kernelSize(src.h);
   const uint64_t total = uint64_t(dst.w) * dst.h;
   const uint64_t limit = min(total, p.groups * 128u);
@@ -190,9 +198,9 @@ __global__ void __launch_bounds__(kThreads) portableGeneral2Kernel(DispatchParam
   __syncthreads();
   const TexelIO<P> io = makeIO<P>(&tabs);
   constexpr uint32_t B = TexelIO<P>::kBytes;
-  const LevelView& l0 = p.lv[0];
-  const LevelView& l1 = p.lv[1];
-  const LevelView& l2 = p.lv[2];
+  const LevelView l0 = levelOf(p, 0);
+  const LevelView l1 = levelOf(p, 1);
+  const LevelView l2 = levelOf(p, 2);
   const uint32_t kx = kernelSize(l0.w), ky = kernelSize(l0.h);
   const uint32_t fkx = kernelSize(l1.w), fky = kernelSize(l1.h);
   const uint32_t tilesX = (l2.w + kG2Tile - 1) / kG2Tile, tilesY = (l2.h + kG2Tile - 1) / kG2Tile;
@@ -232,17 +240,17 @@ cudaError_t launchPreset(const DispatchParams& p, cudaStream_t stream, uint32_t*
     const uint32_t coverW = (p.lv[0].w >> n) << n, coverH = (p.lv[0].h >> n) << n;
     const uint64_t regions = uint64_t((coverW + kRegion - 1) / kRegion) * ((coverH + kRegion - 1) / kRegion);
     if (regions == 0 || p.groups == 0) return cudaSuccess;
-    portableFastKernel<P><<<dim3(uint32_t(regions)), kThreads, 0, stream>>>(p);
+    portableFastKernel<P><<<dim3(uint32_t(regions), 1, p.batch), kThreads, 0, stream>>>(p);
   } else if (p.levelCount == 1) {
     const uint64_t total = uint64_t(p.lv[1].w) * p.lv[1].h;
     const uint64_t work = std::min<uint64_t>(total, p.groups * 128u);
     if (work == 0) return cudaSuccess;
     const uint64_t blocks = std::min<uint64_t>((work + kThreads - 1) / kThreads, 152u * 64u);
-    portableGeneral1Kernel<P><<<dim3(uint32_t(blocks)), kThreads, 0, stream>>>(p);
+    portableGeneral1Kernel<P><<<dim3(uint32_t(blocks), 1, p.batch), kThreads, 0, stream>>>(p);
   } else {
     const uint64_t tiles = uint64_t((p.lv[2].w + kG2Tile - 1) / kG2Tile) * ((p.lv[2].h + kG2Tile - 1) / kG2Tile);
     if (p.groups == 0) return cudaSuccess;
-    portableGeneral2Kernel<P><<<dim3(uint32_t(tiles)), kThreads, 0, stream>>>(p);
+    portableGeneral2Kernel<P><<<dim3(uint32_t(tiles), 1, p.batch), kThreads, 0, stream>>>(p);
   }
   ++*launches;
   return cudaGetLastError();

@@ -24,3 +24,22 @@ def chain_bytes(w: int, h: int, bpp: int = 4) -> int:
         x, y = max(x >> 1, 1), max(y >> 1, 1)
         total += x * y
     return total * bpp
+
+
+def smooth_field(w: int, h: int, seed: int, opaque: bool = False) -> np.ndarray:
+    """[h, w, 4] uint8: per colour channel a sum of 8 random-phase sinusoids
+    (wavelengths log-uniform in 8..512 px) plus uniform +-16 noise around 128;
+    alpha a radial gradient (255 at the centre), or 255 if opaque."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    img = np.zeros((h, w, 4))
+    for c in range(3):
+        acc = np.zeros((h, w))
+        for _ in range(8):
+            lam = np.exp(rng.uniform(np.log(8), np.log(512)))
+            th = rng.uniform(0, 2 * np.pi)
+            acc += np.sin(2 * np.pi * (x * np.cos(th) + y * np.sin(th)) / lam + rng.uniform(0, 2 * np.pi))
+        img[..., c] = 128 + 14 * acc + rng.uniform(-16, 16, (h, w))
+    r = np.hypot(x - w / 2, y - h / 2) / max(np.hypot(w / 2, h / 2), 1)
+    img[..., 3] = 255 if opaque else 255 * (1 - r)
+    return np.clip(np.rint(img), 0, 255).astype(np.uint8)
