@@ -386,6 +386,11 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch ba
                                                             const NvproPyramidImage* images,
                                                             uint32_t imageCount, uint32_t mipLevels);
 
+/* Fix the work-unit size of general-pipeline dispatches (rows of level L+2
+ * per strip; 0 = the default, or the autotuner's choice with
+ * NVPRO_PYRAMID_BATCH_AUTOTUNE) for the following nvproPyramidBatchBuild. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchSetStripBand(NvproPyramidBatch batch, uint32_t band);
+
 /* Generate levels 1.. of every image of the batch on `stream` (no
  * allocation, no host synchronisation).  Launches of one batch must not
  * overlap on the GPU: they share the batch's work counters. */

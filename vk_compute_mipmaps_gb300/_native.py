@@ -132,6 +132,7 @@ SIGNATURES = {
     "nvproPyramidCreateBatch": (c_int, [c_int, c_uint32, POINTER(c_void_p)]),
     "nvproPyramidDestroyBatch": (None, [c_void_p]),
     "nvproPyramidBatchBuild": (c_int, [c_void_p, c_void_p, POINTER(NvproPyramidImage), c_uint32, c_uint32]),
+    "nvproPyramidBatchSetStripBand": (c_int, [c_void_p, c_uint32]),
     "nvproPyramidBatchLaunch": (c_int, [c_void_p, c_void_p]),
     "nvproPyramidBatchGetInfo": (c_int, [c_void_p, POINTER(NvproPyramidBatchInfo)]),
     "nvproPyramidBatchDeviceStatus": (c_int, [c_void_p]),

@@ -914,7 +914,7 @@ namespace {
 
 constexpr uint32_t kBatchMagic = 0x4E50424Du;  // 'NPBM'
 constexpr uint32_t kBandCandidates[] = {4, 8, 16, 32};
-constexpr uint32_t kDefaultStripBand = 8;
+constexpr uint32_t kDefaultStripBand = 16;
 
 // Autotuner cache: strip band by size class (device, mip levels and the
 // histogram of log2(max side) over the batch, counts rounded to powers of two).
@@ -954,6 +954,7 @@ struct NvproPyramidBatch_T {
   uint64_t devBytes = 0;
   uint32_t imageCount = 0;
   uint32_t stripBand = kDefaultStripBand;
+  uint32_t fixedBand = 0;  // nvproPyramidBatchSetStripBand: overrides default and autotuner
   uint32_t autotuned = 0, fromCache = 0;
   cudaStream_t captureStream = nullptr;
   cudaGraph_t graph = nullptr;
@@ -1040,7 +1041,9 @@ NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch b, NvproPyramidStrea
   b->autotuned = b->fromCache = 0;
   uint32_t band = kDefaultStripBand;
   cudaError_t e = cudaSuccess;
-  if (b->flags & NVPRO_PYRAMID_BATCH_AUTOTUNE) {
+  if (b->fixedBand) {
+    band = b->fixedBand;
+  } else if (b->flags & NVPRO_PYRAMID_BATCH_AUTOTUNE) {
     const std::string key = sizeClassKey(images, imageCount, mipLevels);
     bool cached = false;
     {
@@ -1052,8 +1055,9 @@ NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch b, NvproPyramidStrea
       }
     }
     if (!cached) {
-      // Time each candidate on `stream` (a warm-up run, then the median of
-      // three) -- the real work, writing the images' levels.
+      // Time each candidate on `stream` (two warm-up runs, then the median of
+      // five) -- the real work, writing the images' levels.
+      constexpr int kWarm = 2, kTimed = 5;
       float best = 0;
       cudaEvent_t ev[2];
       e = cudaEventCreate(&ev[0]);
@@ -1062,17 +1066,18 @@ NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch b, NvproPyramidStrea
         if (e != cudaSuccess) break;
         e = b->planAndUpload(imgs, c, s);
         uint32_t launches = 0;
-        float t[3] = {};
-        for (int it = 0; it < 4 && e == cudaSuccess; ++it) {
-          if (it > 0) e = cudaEventRecord(ev[0], s);
+        float t[kTimed] = {};
+        for (int it = 0; it < kWarm + kTimed && e == cudaSuccess; ++it) {
+          const bool timed = it >= kWarm;
+          if (timed) e = cudaEventRecord(ev[0], s);
           if (e == cudaSuccess) e = nvpyr::launchBatch(b->dev, s, &launches);
-          if (e == cudaSuccess && it > 0) e = cudaEventRecord(ev[1], s);
-          if (e == cudaSuccess && it > 0) e = cudaEventSynchronize(ev[1]);
-          if (e == cudaSuccess && it > 0) e = cudaEventElapsedTime(&t[it - 1], ev[0], ev[1]);
+          if (e == cudaSuccess && timed) e = cudaEventRecord(ev[1], s);
+          if (e == cudaSuccess && timed) e = cudaEventSynchronize(ev[1]);
+          if (e == cudaSuccess && timed) e = cudaEventElapsedTime(&t[it - kWarm], ev[0], ev[1]);
         }
-        std::sort(t, t + 3);
-        if (e == cudaSuccess && (best == 0 || t[1] < best)) {
-          best = t[1];
+        std::sort(t, t + kTimed);
+        if (e == cudaSuccess && (best == 0 || t[kTimed / 2] < best)) {
+          best = t[kTimed / 2];
           band = c;
         }
       }
@@ -1108,6 +1113,13 @@ NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch b, NvproPyramidStrea
     }
   }
   b->built = true;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidBatchSetStripBand(NvproPyramidBatch b, uint32_t band) {
+  if (!validBatch(b)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid batch object");
+  if (band > 4096) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "strip band %u > 4096", band);
+  b->fixedBand = band;
   return NVPRO_PYRAMID_SUCCESS;
 }
 

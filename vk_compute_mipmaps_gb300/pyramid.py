@@ -269,6 +269,10 @@ class Batch:
         self._images = arr  # the library copies them; kept for inspection
         N.check(self._lib.nvproPyramidBatchBuild(self._h, stream, arr, len(chains), mip_levels), "batch build")
 
+    def set_strip_band(self, band: int) -> None:
+        """Fix the general-pipeline unit size for the next build (0: default / autotuned)."""
+        N.check(self._lib.nvproPyramidBatchSetStripBand(self._h, band), "batch strip band")
+
     def launch(self, stream: Optional[int] = None) -> None:
         import torch
         if stream is None:
