@@ -442,10 +442,8 @@ def run_ours(args, rank, world):
         base_host.copy_(chain.storage[:chain.offsets[1]])
         out_host = torch.empty(chain.offsets[-1] - chain.offsets[1], dtype=torch.uint8, pin_memory=True)
 
-        def e2e_step():
-            chain.storage[:chain.offsets[1]].copy_(base_host, non_blocking=True)
-            run()
-            out_host.copy_(chain.storage[chain.offsets[1]:], non_blocking=True)
+        def e2e_step():  # the public host-memory entry point: banded copies overlapped with the chain
+            V.generate_from_host(chain, base_host, out_host, stream=stream.cuda_stream)
 
         n_e2e = max(3, min(args.steps, 20))
         with torch.cuda.stream(stream):

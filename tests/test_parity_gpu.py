@@ -355,3 +355,24 @@ def test_no_device_wait_gave_up(cuda, native):
     P.generate(chain, cmd=cmd)
     N.check(native.nvproPyramidCmdDeviceStatus(cmd.handle), "device status")
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("w,h,bands", [(16384, 16384, 8), (1920, 1080, 8), (2052, 2052, 5), (2048, 512, 3),
+                                       (4095, 4095, 8), (64, 64, 8)])
+def test_generate_from_host_equals_device_path(cuda, w, h, bands):
+    """Banded host copies overlapped with the chain write the bytes of
+    copy-in + generate + copy-out (the fast first dispatch is tile-local)."""
+    import torch
+    chain = P.MipChain(w, h, N.PRESET_SRGBA8, device=cuda)
+    n0 = chain.offsets[1]
+    g = torch.Generator().manual_seed(w + h)
+    base_host = torch.randint(0, 256, (n0,), generator=g, dtype=torch.uint8).pin_memory()
+    out_host = torch.full((chain.offsets[-1] - n0,), SENTINEL, dtype=torch.uint8).pin_memory()
+    P.generate_from_host(chain, base_host, out_host, bands=bands)
+    torch.cuda.synchronize()
+    ref = P.MipChain(w, h, N.PRESET_SRGBA8, device=cuda)
+    ref.storage[:n0].copy_(base_host)
+    P.generate(ref)
+    torch.cuda.synchronize()
+    assert torch.equal(out_host, ref.storage[n0:].cpu())
+    assert torch.equal(chain.storage[:n0].cpu(), base_host)

@@ -10,10 +10,10 @@ from ._native import (BATCH_AUTOTUNE, BATCH_GRAPH, CMD_NO_FUSION, CMD_PORTABLE_K
                       PRESET_RGBA16F, PRESET_RGBA32F, PRESET_SRGBA8, NativeLibraryError, NvproPyramidImage,
                       NvproPyramidState)
 from .pyramid import (Batch, Cmd, MipChain, Pipelines, cmd_pyramid_dispatch, full_level_count, generate,
-                      level_sizes, make_image, pack_chains, packed_offsets, wrap_dispatcher)
+                      generate_from_host, level_sizes, make_image, pack_chains, packed_offsets, wrap_dispatcher)
 
 __all__ = [
-    "BATCH_AUTOTUNE", "BATCH_GRAPH", "Batch", "pack_chains", "CMD_NO_FUSION", "CMD_PORTABLE_KERNELS", "CMD_RECORD_ONLY", "PRESET_RGBA16F", "PRESET_RGBA32F",
+    "BATCH_AUTOTUNE", "BATCH_GRAPH", "Batch", "pack_chains", "generate_from_host", "CMD_NO_FUSION", "CMD_PORTABLE_KERNELS", "CMD_RECORD_ONLY", "PRESET_RGBA16F", "PRESET_RGBA32F",
     "PRESET_SRGBA8", "NativeLibraryError", "NvproPyramidImage", "NvproPyramidState", "Cmd", "MipChain",
     "Pipelines", "cmd_pyramid_dispatch", "full_level_count", "generate", "level_sizes", "make_image",
     "packed_offsets", "wrap_dispatcher",

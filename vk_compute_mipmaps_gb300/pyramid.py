@@ -248,6 +248,104 @@ def generate(chain: MipChain, stream: Optional[int] = None, mip_levels: int = 0,
     return cmd.launch_count
 
 
+_copy_streams_cache: dict = {}
+
+
+def _copy_streams(dev):
+    """Two side streams per device for host copies (created once)."""
+    import torch
+    key = (threading.get_ident(), str(dev))
+    if key not in _copy_streams_cache:
+        _copy_streams_cache[key] = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+    return _copy_streams_cache[key]
+
+
+def _first_fast_levels(w: int, h: int, levels: int) -> int:
+    """Levels of the first dispatch if the default schedule starts with a fast
+    dispatch (nvproPyramidDefaultFastDispatcher<4, 6>: both sizes divisible by
+    4, as many halvings as both stay even, at most 6), else 0."""
+    if w % 4 or h % 4:
+        return 0
+    n = 0
+    while w % 2 == 0 and h % 2 == 0 and n < levels - 1 and n < 6:
+        w, h, n = w // 2, h // 2, n + 1
+    return n
+
+
+def _sub_image(chain: "MipChain", first: int, count: int, row0: int, rows: int) -> N.NvproPyramidImage:
+    """Levels first..first+count-1 of `chain` restricted to level-`first` rows
+    [row0, row0 + rows) (row ranges of the deeper levels scale by 2^k)."""
+    sizes = level_sizes(chain.width, chain.height, chain.levels)
+    base = chain.storage.data_ptr()
+    ptrs, pitches = [], []
+    for k in range(first, first + count):
+        w = sizes[k][0]
+        pitch = w * chain.bpp
+        ptrs.append(base + chain.offsets[k] + (row0 >> (k - first)) * pitch)
+        pitches.append(pitch)
+    return make_image(ptrs, sizes[first][0], rows, pitches)
+
+
+def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Optional[int] = None, bands: int = 8,
+                       flags: int = 0) -> None:
+    """Level 0 from pinned host memory (`host_base`, chain.offsets[1] bytes),
+    levels 1.. back to pinned host memory (`host_levels`, the rest of the
+    packed chain), with the copies overlapped with the generation.
+
+    When the chain starts with a fast dispatch of n levels, that dispatch is
+    local to 2^n-row tiles, so level 0 goes in as row bands (multiples of 2^n
+    rows): the band's dispatch runs while the next band is copied in and the
+    previous band's levels 1..n are copied out; the remaining dispatches run
+    on level n after the last band.  The dispatches, and so the bytes, are
+    those of `generate` on the whole chain.  Otherwise: copy in, generate,
+    copy out.  Returns when the work is queued; `stream` (default: torch's
+    current stream) waits for all of it."""
+    import torch
+    dev = chain.storage.device
+    cur = torch.cuda.current_stream(dev) if stream is None else torch.cuda.ExternalStream(stream, device=dev)
+    off = chain.offsets
+    n = _first_fast_levels(chain.width, chain.height, chain.levels)
+    rows_unit = 1 << n
+    band_rows = -(-chain.height // max(bands, 1) // rows_unit) * rows_unit if n else chain.height
+    if not n or bands <= 1 or band_rows >= chain.height:
+        chain.storage[:off[1]].copy_(host_base, non_blocking=True)
+        generate(chain, stream=cur.cuda_stream, flags=flags)
+        host_levels.copy_(chain.storage[off[1]:off[-1]], non_blocking=True)
+        return
+    lib = N.load()
+    p, c = _defaults(chain.preset, flags)
+    copy_in, copy_out = _copy_streams(dev)
+    copy_in.wait_stream(cur)
+    copy_out.wait_stream(cur)
+    pitch0 = chain.width * chain.bpp
+    sizes = level_sizes(chain.width, chain.height, chain.levels)
+    r0 = 0
+    while r0 < chain.height:
+        rows = min(band_rows, chain.height - r0)
+        a, b = r0 * pitch0, (r0 + rows) * pitch0
+        with torch.cuda.stream(copy_in):
+            chain.storage[a:b].copy_(host_base[a:b], non_blocking=True)
+        cur.wait_stream(copy_in)
+        img = _sub_image(chain, 0, n + 1, r0, rows)
+        N.check(lib.nvproPyramidGenerate(c.handle, cur.cuda_stream, p.struct, ctypes.byref(img), n + 1),
+                "nvproPyramidGenerate")
+        copy_out.wait_stream(cur)
+        with torch.cuda.stream(copy_out):
+            for k in range(1, n + 1):
+                pk = sizes[k][0] * chain.bpp
+                lo, hi = off[k] + (r0 >> k) * pk, off[k] + ((r0 + rows) >> k) * pk
+                host_levels[lo - off[1]:hi - off[1]].copy_(chain.storage[lo:hi], non_blocking=True)
+        r0 += rows
+    if n + 1 < chain.levels:  # the rest of the schedule, from level n
+        img = _sub_image(chain, n, chain.levels - n, 0, sizes[n][1])
+        N.check(lib.nvproPyramidGenerate(c.handle, cur.cuda_stream, p.struct, ctypes.byref(img), chain.levels - n),
+                "nvproPyramidGenerate")
+        copy_out.wait_stream(cur)
+        with torch.cuda.stream(copy_out):
+            host_levels[off[n + 1] - off[1]:].copy_(chain.storage[off[n + 1]:off[-1]], non_blocking=True)
+    cur.wait_stream(copy_out)
+
+
 class Batch:
     """Many sRGBA8 chains generated by one persistent launch
     (nvproPyramidCreateBatch / BatchBuild / BatchLaunch)."""
