@@ -82,6 +82,39 @@ typedef struct NvproPyramidPipeline_T* NvproPyramidPipeline;
  * vkCreateComputePipelines calls of minimal_app/minimal_mipmaps.cpp:178-190. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCreatePipeline(
     NvproPyramidPreset preset, uint32_t isFastPipeline, NvproPyramidPipeline* pPipeline);
+
+/* Pipeline configuration bits: the macros the reference's demo prepends to
+ * the shader source per pipeline (demo_app/mipmap_pipelines.cpp:107-122),
+ * with the values of demo_app/pipeline_alternative.hpp:38-43.
+ *
+ * SRGB_SHARED / F16_SHARED (srgba8_mipmap_preamble.glsl:60-108; sRGBA8
+ * preset only, at most one of the two): the values a dispatch hands from one
+ * level to the next through shared memory are kept in a compact format.  Those
+ * are level L+3 of a fast dispatch of 4 or 5 levels, level L+4 of a 6-level
+ * fast dispatch (sharedTile_, nvpro_pyramid.glsl:253,395,487-512) and level
+ * L+1 of a 2-level general dispatch (sharedLevel_, :555,664,717).  The levels
+ * after the hand-off are reduced from the compact values; the hand-off level
+ * itself is stored from its FP32 values, as in the reference.
+ *   SRGB_SHARED: the texel's sRGBA8 code (the preset's own store encoding)
+ *   decoded again with the preset's load tables.  The reference's srgbPack /
+ *   srgbUnpack compute the same code with pow() and packUnorm4x8, whose
+ *   precision and rounding of halves GLSL leaves to the implementation; the
+ *   exact codec is the pinned reading.
+ *   F16_SHARED: each channel rounded to binary16 (round to nearest even).
+ *
+ * NO_BILINEAR (srgba8_mipmap_preamble.glsl:40-58): LOAD_REDUCE4 as four
+ * texel loads instead of one bilinear sample.  Every pipeline of this library
+ * computes it that way (hardware bilinear filtering precision is
+ * implementation-defined), so the bit is accepted and changes nothing. */
+#define NVPRO_PYRAMID_CONFIG_SRGB_SHARED 0x1u
+#define NVPRO_PYRAMID_CONFIG_F16_SHARED  0x2u
+#define NVPRO_PYRAMID_CONFIG_NO_BILINEAR 0x4u
+
+/* nvproPyramidCreatePipeline with configuration bits (0 = the default
+ * pipeline).  UNSUPPORTED for a shared format on a preset other than sRGBA8;
+ * INVALID_ARGUMENT for both shared formats or an unknown bit. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCreatePipelineEx(
+    NvproPyramidPreset preset, uint32_t isFastPipeline, uint32_t configBits, NvproPyramidPipeline* pPipeline);
 NVPRO_PYRAMID_API void nvproPyramidDestroyPipeline(NvproPyramidPipeline pipeline);
 
 /* Bytes per texel of a preset (0 for an unknown preset). */
@@ -185,6 +218,7 @@ typedef struct NvproPyramidDispatchRecord {
   uint32_t groupCountZ;
   uint32_t pipelineBound;  /* a bind preceded this dispatch */
   uint32_t barrierBefore;  /* a barrier preceded this dispatch */
+  uint32_t configBits;     /* NVPRO_PYRAMID_CONFIG_* of the bound pipeline */
 } NvproPyramidDispatchRecord;
 
 NVPRO_PYRAMID_API uint32_t nvproPyramidCmdRecordCount(NvproPyramidCmd cmd);

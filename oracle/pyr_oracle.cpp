@@ -262,15 +262,50 @@ char fastOrder(uint32_t n, uint32_t k) {
   return 'H';
 }
 
+// Shared-memory formats of the sRGBA8 preset (srgba8_mipmap_preamble.glsl:60-108).
+enum SharedFormat { kSharedFp32 = 0, kSharedSrgb = 1, kSharedF16 = 2 };
+
+// The level (relative to L) whose values an n-level dispatch hands on through
+// shared memory, 0 if none.  Fast: handleTile_ fills subLevelCount_ = 4 (n = 6)
+// or 3 (n = 4, 5) levels and writes the last one to sharedTile_
+// (nvpro_pyramid.glsl:440-462, :393-396); the tail reads it back (:487-512).
+// General, two levels: level L+1 goes to sharedLevel_ (:717) and level L+2
+// reads it back (:664).
+uint32_t handoffLevel(bool fast, uint32_t n) {
+  if (fast) return n == 6 ? 4 : n >= 4 ? 3 : 0;
+  return n == 2 ? 1 : 0;
+}
+
+// NVPRO_PYRAMID_SHARED_STORE then NVPRO_PYRAMID_SHARED_LOAD of a value.
+// SRGB_SHARED packs the sRGB code (srgbPack, preamble.glsl:91-99) and decodes
+// it again (srgbUnpack, :81-88); GLSL leaves pow()'s precision and the
+// rounding of halves in packUnorm4x8 to the implementation, so the code here
+// is the exact one of the STORE encoding and the decode is the LOAD table.
+// F16_SHARED: f16vec4(v), round to nearest even, and back (:103-108).
+Vec4 sharedRoundTrip(int fmt, const Vec4& v) {
+  if (fmt == kSharedFp32) return v;
+  Vec4 r;
+  if (fmt == kSharedSrgb) {
+    const SrgbTables& t = tables();
+    for (int c = 0; c < 3; ++c) r.v[c] = t.decode[srgbEncode(v.v[c])];
+    r.v[3] = t.alpha[alphaEncode(v.v[3])];
+  } else {
+    for (int c = 0; c < 4; ++c) r.v[c] = halfToFloat(floatToHalf(v.v[c]));
+  }
+  return r;
+}
+
 // Fast pipeline dispatch (nvpro_pyramid.glsl:401-532): levels L+1..L+n from
-// square tiles of edge 2^n of level L; all values inside the dispatch stay FP32.
-void fastDispatch(const Image& img, uint32_t L, uint32_t n, uint64_t groups) {
+// square tiles of edge 2^n of level L; all values inside the dispatch stay FP32
+// except the hand-off level of a pipeline with a shared format (sharedFmt).
+void fastDispatch(const Image& img, uint32_t L, uint32_t n, uint64_t groups, int sharedFmt) {
   const uint32_t W = img.w[L], H = img.h[L];
   const uint32_t T = 1u << n;
   const uint64_t tilesX = W >> n, tilesY = H >> n;
   const uint64_t tilesPerGroup = (n > 5 ? 4096u : 1024u) >> (2 * n);
   const uint64_t limit = std::min<uint64_t>(tilesX * tilesY, groups * std::max<uint64_t>(tilesPerGroup, 1));
   std::vector<Vec4> cur, next;
+  const uint32_t handoff = sharedFmt != kSharedFp32 ? handoffLevel(true, n) : 0;
   for (uint64_t t = 0; t < limit; ++t) {
     const uint32_t tx = (uint32_t)(t % tilesX), ty = (uint32_t)(t / tilesX);
     uint32_t e = T / 2;  // edge of the level L+1 tile
@@ -294,7 +329,7 @@ void fastDispatch(const Image& img, uint32_t L, uint32_t n, uint64_t groups) {
           const Vec4& bl = cur[(size_t)(2 * y + 1) * e + 2 * x];
           const Vec4& br = cur[(size_t)(2 * y + 1) * e + 2 * x + 1];
           Vec4 v = vert ? reduce4(tl, bl, tr, br) : reduce4(tl, tr, bl, br);
-          next[(size_t)y * ne + x] = v;
+          next[(size_t)y * ne + x] = k == handoff ? sharedRoundTrip(sharedFmt, v) : v;
           img.store(L + k, tx * ne + x, ty * ne + y, v);
         }
       cur.swap(next);
@@ -345,7 +380,7 @@ Vec4 reduceSample(Loader&& ld, uint32_t kx, uint32_t ky, uint32_t dstW, uint32_t
 }
 
 // General pipeline dispatch (nvpro_pyramid.glsl:824-882), 1 or 2 levels.
-void generalDispatch(const Image& img, uint32_t L, uint32_t n, uint64_t groups) {
+void generalDispatch(const Image& img, uint32_t L, uint32_t n, uint64_t groups, int sharedFmt) {
   const uint32_t sw = img.w[L], sh = img.h[L];
   const uint32_t w1 = img.w[L + 1], h1 = img.h[L + 1];
   const uint32_t kx = kernelSize(sw), ky = kernelSize(sh);
@@ -379,9 +414,10 @@ void generalDispatch(const Image& img, uint32_t L, uint32_t n, uint64_t groups) 
         if (x >= w1 || y >= h1) continue;
         const size_t idx = (size_t)y * w1 + x;
         if (!have[idx]) {
-          lvl1[idx] = levelSample(x, y);
+          const Vec4 v = levelSample(x, y);
+          lvl1[idx] = sharedRoundTrip(sharedFmt, v);
           have[idx] = 1;
-          img.store(L + 1, x, y, lvl1[idx]);
+          img.store(L + 1, x, y, v);
         }
       }
     for (uint32_t j = 0; j < 8; ++j)
@@ -621,10 +657,14 @@ int orc_default_schedule(uint32_t w, uint32_t h, uint32_t mipLevels, int hasFast
 }
 
 // Run a dispatch sequence (shader semantics) on a packed image whose level 0
-// is filled.  preset: 1 sRGBA8, 2 RGBA32F, 3 RGBA16F.
-int orc_run(int preset, uint32_t w, uint32_t h, uint32_t mipLevels, const uint32_t* isFast, const uint32_t* pc,
-            const uint32_t* groups, int count, uint8_t* packed) {
+// is filled.  preset: 1 sRGBA8, 2 RGBA32F, 3 RGBA16F.  fastShared /
+// generalShared: shared-memory format of the fast / general pipeline
+// (0 FP32, 1 SRGB_SHARED, 2 F16_SHARED; sRGBA8 only).
+int orc_run_ex(int preset, int fastShared, int generalShared, uint32_t w, uint32_t h, uint32_t mipLevels,
+               const uint32_t* isFast, const uint32_t* pc, const uint32_t* groups, int count, uint8_t* packed) {
   if (texelBytes(preset) == 0 || w == 0 || h == 0) return -1;
+  if (fastShared < 0 || fastShared > 2 || generalShared < 0 || generalShared > 2) return -4;
+  if ((fastShared || generalShared) && preset != kSrgba8) return -4;
   if (mipLevels == 0) mipLevels = fullLevels(w, h);
   Image img(preset, w, h, mipLevels, packed);
   for (int i = 0; i < count; ++i) {
@@ -632,13 +672,18 @@ int orc_run(int preset, uint32_t w, uint32_t h, uint32_t mipLevels, const uint32
     if (n == 0 || L + n >= mipLevels) return -2;
     if (isFast[i]) {
       if (n > 6 || (img.w[L] % (1u << n)) || (img.h[L] % (1u << n))) return -3;
-      fastDispatch(img, L, n, groups[i]);
+      fastDispatch(img, L, n, groups[i], fastShared);
     } else {
       if (n > 2) return -3;
-      generalDispatch(img, L, n, groups[i]);
+      generalDispatch(img, L, n, groups[i], generalShared);
     }
   }
   return 0;
+}
+
+int orc_run(int preset, uint32_t w, uint32_t h, uint32_t mipLevels, const uint32_t* isFast, const uint32_t* pc,
+            const uint32_t* groups, int count, uint8_t* packed) {
+  return orc_run_ex(preset, 0, 0, w, h, mipLevels, isFast, pc, groups, count, packed);
 }
 
 // The reference CPU generator (cpuGenerateMipmaps_sRGBA), restated.

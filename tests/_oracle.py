@@ -33,6 +33,8 @@ def orc() -> ctypes.CDLL:
         lib.orc_default_schedule.argtypes = [c_uint32, c_uint32, c_uint32, c_int, c_uint32, c_uint32, u32p, u32p,
                                              u32p, c_int]
         lib.orc_run.argtypes = [c_int, c_uint32, c_uint32, c_uint32, u32p, u32p, u32p, c_int, POINTER(c_uint8)]
+        lib.orc_run_ex.argtypes = [c_int, c_int, c_int, c_uint32, c_uint32, c_uint32, u32p, u32p, u32p, c_int,
+                                   POINTER(c_uint8)]
         lib.orc_refcpu_srgba8.argtypes = [c_uint32, c_uint32, POINTER(c_uint8)]
         lib.orc_f64_pyramid.argtypes = [c_uint32, c_uint32, c_uint32, POINTER(c_double)]
         lib.orc_srgb_tables.argtypes = [POINTER(c_float)] * 3
@@ -69,8 +71,14 @@ def default_schedule(w, h, mips=0, has_fast=True, div=4, max_levels=6):
     return [(a[i], b[i], c[i]) for i in range(cnt)]
 
 
-def run(preset: int, w: int, h: int, packed: np.ndarray, schedule=None, mips: int = 0) -> np.ndarray:
-    """Apply a dispatch schedule (default: the reference's) to a packed image in place."""
+# shared-memory formats of the sRGBA8 pipelines (SRGB_SHARED / F16_SHARED)
+SHARED_FP32, SHARED_SRGB, SHARED_F16 = 0, 1, 2
+
+
+def run(preset: int, w: int, h: int, packed: np.ndarray, schedule=None, mips: int = 0, fast_shared: int = 0,
+        general_shared: int = 0) -> np.ndarray:
+    """Apply a dispatch schedule (default: the reference's) to a packed image in
+    place; fast_shared / general_shared: the pipelines' shared-memory formats."""
     mips = mips or full_levels(w, h)
     if schedule is None:
         schedule = default_schedule(w, h, mips)
@@ -79,7 +87,8 @@ def run(preset: int, w: int, h: int, packed: np.ndarray, schedule=None, mips: in
     for i, (f, pc, g) in enumerate(schedule):
         a[i], b[i], c[i] = f, pc, g
     assert packed.flags.c_contiguous
-    rc = orc().orc_run(preset, w, h, mips, a, b, c, len(schedule), packed.ctypes.data_as(POINTER(c_uint8)))
+    rc = orc().orc_run_ex(preset, fast_shared, general_shared, w, h, mips, a, b, c, len(schedule),
+                          packed.ctypes.data_as(POINTER(c_uint8)))
     assert rc == 0, rc
     return packed
 
@@ -94,10 +103,11 @@ def packed_from_base(preset: int, base: np.ndarray, mips: int = 0) -> np.ndarray
     return buf
 
 
-def pyramid(preset: int, base: np.ndarray, schedule=None, mips: int = 0) -> np.ndarray:
+def pyramid(preset: int, base: np.ndarray, schedule=None, mips: int = 0, fast_shared: int = 0,
+            general_shared: int = 0) -> np.ndarray:
     h, w = base.shape[:2]
     buf = packed_from_base(preset, base, mips)
-    return run(preset, w, h, buf, schedule, mips)
+    return run(preset, w, h, buf, schedule, mips, fast_shared, general_shared)
 
 
 def refcpu(base: np.ndarray) -> np.ndarray:

@@ -165,3 +165,31 @@ def test_partial_mip_count_and_general_only(native):
     recs = record(64, 64, has_fast=False)
     assert all(r["isFastPipeline"] == 0 for r in recs)
     assert sum(r["pushConstant"] & 31 for r in recs) == 6
+
+
+def test_pipeline_config_bits(native):
+    """nvproPyramidCreatePipelineEx: the demo's per-pipeline config bits
+    (demo_app/pipeline_alternative.hpp:40-42) and their validation."""
+    h = ctypes.c_void_p()
+
+    def create(preset, fast, bits):
+        return native.nvproPyramidCreatePipelineEx(preset, fast, bits, ctypes.byref(h))
+
+    assert (N.CONFIG_SRGB_SHARED, N.CONFIG_F16_SHARED, N.CONFIG_NO_BILINEAR) == (1, 2, 4)
+    for bits in (0, 1, 2, 4, 5, 6):
+        assert create(N.PRESET_SRGBA8, 1, bits) == N.SUCCESS, bits
+        native.nvproPyramidDestroyPipeline(h)
+    assert create(N.PRESET_SRGBA8, 0, 3) == N.ERROR_INVALID_ARGUMENT  # both shared formats
+    assert create(N.PRESET_SRGBA8, 0, 8) == N.ERROR_INVALID_ARGUMENT  # unknown bit
+    assert create(N.PRESET_RGBA32F, 0, N.CONFIG_F16_SHARED) == N.ERROR_UNSUPPORTED  # sRGBA8 only
+    assert create(N.PRESET_RGBA32F, 1, N.CONFIG_NO_BILINEAR) == N.SUCCESS
+    native.nvproPyramidDestroyPipeline(h)
+    # each record carries the bits of the pipeline bound for it
+    cmd = P.Cmd(N.CMD_RECORD_ONLY)
+    pipes = P.Pipelines(general_config=N.CONFIG_SRGB_SHARED, fast_config=N.CONFIG_F16_SHARED)
+    cmd.begin(None)
+    cmd.bind_image(fake_image(2052, 2052))
+    P.cmd_pyramid_dispatch(cmd, pipes, 2052, 2052)
+    cmd.end()
+    recs = cmd.records()
+    assert [(r["isFastPipeline"], r["configBits"]) for r in recs] == [(1, 2), (0, 1), (1, 2), (0, 1)]

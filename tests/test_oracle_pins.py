@@ -10,7 +10,13 @@
   code of them.
 * Shader semantics (the oracle's main mode) must stay within the reference's
   own delta bar against its CPU generator (demo_app/rtx3090.json: 2 on opaque
-  images, 4-5 with alpha).
+  images, 4-5 with alpha), with the default pipelines and with the
+  shared-memory formats SRGB_SHARED / F16_SHARED (the same file reports the
+  same bar for its srgbShared / f16Shared alternatives).
+* The shared formats are pinned structurally: with SRGB_SHARED a two-level
+  general dispatch equals two one-level ones and a four-level fast dispatch
+  equals a three-level one followed by a one-level one (same operation order,
+  same quantisation points).
 """
 import gzip
 import json
@@ -167,3 +173,75 @@ def test_float_oracle_close_to_fp64():
     f64 = O.f64_pyramid(base)
     for a, b in zip(f32, f64):
         assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-3)) < 1e-5
+
+
+def test_float_to_half_matches_numpy():
+    # F16_SHARED rounds to binary16, nearest even (numpy's float -> float16 rule)
+    lib = O.orc()
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([rng.random(20000, dtype=np.float32), rng.random(5000, dtype=np.float32) * 1e-4,
+                         np.float32([0.0, 1.0, 6.1035156e-05, 5.9604645e-08, 2.9802322e-08, 65504.0, 65520.0]),
+                         (np.arange(1, 2049, dtype=np.float32) + 0.5) * np.float32(2.0 ** -24),  # subnormal ties
+                         (np.arange(1024, 2048, dtype=np.float32) + 0.5) / np.float32(1024.0)])  # normal ties
+    with np.errstate(over="ignore"):  # 65520 rounds to infinity
+        want = xs.astype(np.float16)
+    mine = np.array([lib.orc_float_to_half(float(x)) for x in xs], np.uint16)
+    assert np.array_equal(mine, want.view(np.uint16))
+    back = np.array([lib.orc_half_to_float(int(v)) for v in mine], np.float32)
+    assert np.array_equal(back, want.astype(np.float32))
+
+
+@pytest.mark.parametrize("w,h", [(256, 256), (255, 255), (192, 108), (2052, 20), (64, 1024)])
+@pytest.mark.parametrize("fmt", [O.SHARED_SRGB, O.SHARED_F16])
+def test_shared_formats_within_reference_delta_bar(w, h, fmt):
+    for opaque, bar in ((True, 2), (False, 5)):
+        base = smooth_field(w, h, w * 3 + h, opaque)
+        got = O.pyramid(1, base, fast_shared=fmt, general_shared=fmt)
+        delta = O.worst_delta(got, O.refcpu(base), w, h)
+        assert delta <= bar, (w, h, fmt, opaque, delta)
+
+
+def test_shared_formats_change_bytes_negative_control():
+    # the hand-off quantisation is visible: every variant differs from the
+    # default somewhere, and only from the first level after the hand-off
+    base = np.random.default_rng(8).integers(0, 256, (256, 256, 4), dtype=np.uint8)
+    off = O.offsets(256, 256, O.full_levels(256, 256), 4)
+    ref = O.pyramid(1, base)  # F6 F2
+    for fmt in (O.SHARED_SRGB, O.SHARED_F16):
+        got = O.pyramid(1, base, fast_shared=fmt)
+        assert np.array_equal(got[:off[5]], ref[:off[5]])  # levels 0..4 (the hand-off level included)
+        assert not np.array_equal(got[off[5]:off[6]], ref[off[5]:off[6]])
+    base = smooth_field(255, 255, 3, False)
+    ref = O.pyramid(1, base)  # G2 x3, G1
+    off = O.offsets(255, 255, O.full_levels(255, 255), 4)
+    for fmt in (O.SHARED_SRGB, O.SHARED_F16):
+        got = O.pyramid(1, base, general_shared=fmt)
+        assert np.array_equal(got[:off[2]], ref[:off[2]])
+        assert not np.array_equal(got[off[2]:], ref[off[2]:])
+
+
+def split_schedule(w, h, mips=0):
+    """The default schedule with every G2 split into G1 G1 and every F4 into
+    F3 F1 (full workgroup counts)."""
+    out = []
+    for fast, pc, _ in O.default_schedule(w, h, mips):
+        L, n = pc >> 5, pc & 31
+        parts = [3, 1] if (fast and n == 4) else [1, 1] if (not fast and n == 2) else [n]
+        for k in parts:
+            lw, lh = max(w >> L, 1), max(h >> L, 1)
+            if fast:
+                groups = (lw * lh + (4095 if k > 5 else 1023)) >> (12 if k > 5 else 10)
+            else:
+                dw, dh = max(lw >> k, 1), max(lh >> k, 1)
+                groups = (dw * dh + 127) // 128
+            out.append((fast, L << 5 | k, groups))
+            L += k
+    return out
+
+
+@pytest.mark.parametrize("w,h,mips", [(255, 255, 0), (1023, 777, 0), (96, 3, 0), (208, 48, 0), (48, 80, 0), (16, 16, 0)])
+def test_srgb_shared_equals_split_dispatches(w, h, mips):
+    base = smooth_field(w, h, w + 2 * h, False)
+    got = O.pyramid(1, base, mips=mips, fast_shared=O.SHARED_SRGB, general_shared=O.SHARED_SRGB)
+    want = O.pyramid(1, base, schedule=split_schedule(w, h, mips), mips=mips)
+    assert np.array_equal(got, want)

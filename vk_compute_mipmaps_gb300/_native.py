@@ -31,6 +31,10 @@ CMD_RECORD_ONLY = 0x1
 CMD_NO_FUSION = 0x2
 CMD_PORTABLE_KERNELS = 0x4
 
+CONFIG_SRGB_SHARED = 0x1
+CONFIG_F16_SHARED = 0x2
+CONFIG_NO_BILINEAR = 0x4
+
 
 class NvproPyramidImage(ctypes.Structure):
     _fields_ = [
@@ -71,6 +75,7 @@ class NvproPyramidDispatchRecord(ctypes.Structure):
         ("groupCountZ", c_uint32),
         ("pipelineBound", c_uint32),
         ("barrierBefore", c_uint32),
+        ("configBits", c_uint32),
     ]
 
 
@@ -99,6 +104,7 @@ SIGNATURES = {
     "nvproPyramidResultString": (c_char_p, [c_int]),
     "nvproPyramidLastError": (c_char_p, []),
     "nvproPyramidCreatePipeline": (c_int, [c_int, c_uint32, POINTER(c_void_p)]),
+    "nvproPyramidCreatePipelineEx": (c_int, [c_int, c_uint32, c_uint32, POINTER(c_void_p)]),
     "nvproPyramidDestroyPipeline": (None, [c_void_p]),
     "nvproPyramidPresetTexelBytes": (c_uint32, [c_int]),
     "nvproPyramidFullLevelCount": (c_uint32, [c_uint32, c_uint32]),

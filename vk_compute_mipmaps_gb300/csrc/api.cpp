@@ -53,6 +53,7 @@ struct NvproPyramidPipeline_T {
   uint32_t magic;
   uint32_t preset;
   uint32_t isFast;
+  uint32_t configBits;
 };
 
 struct Record {
@@ -122,6 +123,9 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
   out->inputLevel = L;
   out->levelCount = n;
   out->groups = (rec.info.groupCountY == 0 || rec.info.groupCountZ == 0) ? 0 : rec.info.groupCountX;
+  out->sharedFmt = (rec.info.configBits & NVPRO_PYRAMID_CONFIG_SRGB_SHARED)  ? kSharedSrgb
+                   : (rec.info.configBits & NVPRO_PYRAMID_CONFIG_F16_SHARED) ? kSharedF16
+                                                                             : kSharedFp32;
   const uint32_t align = bpp == 4 ? 4 : bpp == 8 ? 8 : 16;
   for (uint32_t k = 0; k <= n; ++k) {
     const uint32_t lvl = L + k;
@@ -164,11 +168,24 @@ uint32_t nvproPyramidPresetTexelBytes(NvproPyramidPreset preset) { return preset
 
 NvproPyramidResult nvproPyramidCreatePipeline(NvproPyramidPreset preset, uint32_t isFastPipeline,
                                               NvproPyramidPipeline* pPipeline) {
+  return nvproPyramidCreatePipelineEx(preset, isFastPipeline, 0, pPipeline);
+}
+
+NvproPyramidResult nvproPyramidCreatePipelineEx(NvproPyramidPreset preset, uint32_t isFastPipeline,
+                                                uint32_t configBits, NvproPyramidPipeline* pPipeline) {
   if (!pPipeline) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pPipeline is NULL");
   *pPipeline = nullptr;
   if (presetBytes(uint32_t(preset)) == 0)
     return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "unknown preset %d", int(preset));
-  auto* p = new (std::nothrow) NvproPyramidPipeline_T{kPipelineMagic, uint32_t(preset), isFastPipeline ? 1u : 0u};
+  constexpr uint32_t kShared = NVPRO_PYRAMID_CONFIG_SRGB_SHARED | NVPRO_PYRAMID_CONFIG_F16_SHARED;
+  if (configBits & ~(kShared | NVPRO_PYRAMID_CONFIG_NO_BILINEAR))
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "unknown configuration bits 0x%x", configBits);
+  if ((configBits & kShared) == kShared)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "SRGB_SHARED and F16_SHARED are exclusive");
+  if ((configBits & kShared) && preset != NVPRO_PYRAMID_PRESET_SRGBA8)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "shared-memory formats exist for the sRGBA8 preset only");
+  auto* p = new (std::nothrow)
+      NvproPyramidPipeline_T{kPipelineMagic, uint32_t(preset), isFastPipeline ? 1u : 0u, configBits};
   if (!p) return fail(NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY, "host allocation failed");
   *pPipeline = p;
   return NVPRO_PYRAMID_SUCCESS;
@@ -325,6 +342,7 @@ NvproPyramidResult nvproPyramidCmdDispatch(NvproPyramidCmd cmd, uint32_t gx, uin
   std::memset(&r, 0, sizeof r);
   r.info.isFastPipeline = cmd->pipeline->isFast;
   r.info.preset = cmd->pipeline->preset;
+  r.info.configBits = cmd->pipeline->configBits;
   r.info.pushConstant = cmd->pushConstant;
   r.info.groupCountX = gx;
   r.info.groupCountY = gy;
@@ -404,7 +422,9 @@ NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
     } else if (!portableOnly && generalFastSupported(p)) {
       // A run of general dispatches is one launch (fused unless NO_FUSION).
       size_t j = i + 1;
-      while (fuse && j < params.size() && j - i < generalMaxStages() && generalFastSupported(params[j])) ++j;
+      while (fuse && j < params.size() && j - i < generalMaxStages() && generalFastSupported(params[j]) &&
+             params[j].sharedFmt == p.sharedFmt)
+        ++j;
       e = launchGeneralChain(&params[i], uint32_t(j - i), cmd->stream, cmd->scratch, &cmd->launches);
       i = j;
     } else {

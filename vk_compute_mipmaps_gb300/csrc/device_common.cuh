@@ -163,6 +163,13 @@ struct TexelIO<kRgba16f> {
   }
 };
 
+// F16_SHARED (srgba8_mipmap_preamble.glsl:103-108): f16vec4(v) and back;
+// each channel rounded to binary16, nearest even.
+__device__ __forceinline__ float4 f16RoundTrip(float4 v) {
+  return make_float4(__half2float(__float2half_rn(v.x)), __half2float(__float2half_rn(v.y)),
+                     __half2float(__float2half_rn(v.z)), __half2float(__float2half_rn(v.w)));
+}
+
 __device__ __forceinline__ uint8_t* texelAddr(const LevelView& v, uint32_t x, uint32_t y, uint32_t bytes) {
   return v.ptr + (uint64_t)y * v.pitch + (uint64_t)x * bytes;
 }

@@ -117,7 +117,10 @@ __device__ __forceinline__ float4 decodeAligned(uint32_t w, const Lut& L) {
 // from level L along x / y (else two taps); TX1 / TY1: the same from level
 // L+1 (two levels only).  The flags are uniform across the grid, so their
 // branches never diverge; one code path for all of them keeps the chain
-// kernel free of calls.
+// kernel free of calls.  SF: the pipeline's shared format, applied to the
+// level-(L+1) values that level L+2 is reduced from (sharedLevel_,
+// nvpro_pyramid.glsl:664,717).
+template <uint32_t SF>
 __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t band, uint32_t lane, const Lut& lut) {
   const uint32_t LEVELS = st.variant >= 16 ? 1u : 2u;
   const bool TX0 = LEVELS == 2 ? (st.variant & 8) != 0 : (st.variant & 2) != 0;
@@ -220,8 +223,11 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
         l1 = reduce3p(wx, va, vb, shflDown(va, 1));
       else
         l1 = reduce2p(va, vb);
-      storeIf(store1x && y < yStoreEnd, p.dst1 + uint64_t(y) * p.pitch1 + uint64_t(x) * 4, encodeTexel(l1, L));
+      const uint32_t code1 = encodeTexel(l1, L);
+      storeIf(store1x && y < yStoreEnd, p.dst1 + uint64_t(y) * p.pitch1 + uint64_t(x) * 4, code1);
       if (LEVELS == 2) {
+        if (SF == kSharedSrgb) l1 = decodeAligned(code1, L);
+        if (SF == kSharedF16) l1 = f16RoundTrip(l1);
         const uint32_t jj = y - yb;
         bool emit = false;
         uint32_t Y = 0;

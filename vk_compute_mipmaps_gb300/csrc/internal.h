@@ -10,6 +10,18 @@ constexpr uint32_t kMaxDispatchLevels = 6;  // fast pipeline: 1..6 levels (nvpro
 
 enum Preset : uint32_t { kSrgba8 = 1, kRgba32f = 2, kRgba16f = 3 };
 
+// Shared-memory formats of the sRGBA8 preset (srgba8_mipmap_preamble.glsl:60-108).
+enum SharedFormat : uint32_t { kSharedFp32 = 0, kSharedSrgb = 1, kSharedF16 = 2 };
+
+// The level (relative to the input level) whose values a dispatch of n levels
+// hands on through shared memory, or 0 if none: L+3 for fast dispatches of 4
+// or 5 levels, L+4 for 6 levels (nvpro_pyramid.glsl:440-462), L+1 for
+// two-level general dispatches (:717).
+inline __host__ __device__ uint32_t sharedHandoffLevel(bool isFast, uint32_t n) {
+  if (isFast) return n == 6 ? 4u : n >= 4 ? 3u : 0u;
+  return n == 2 ? 1u : 0u;
+}
+
 inline uint32_t presetBytes(uint32_t preset) {
   return preset == kSrgba8 ? 4u : preset == kRgba32f ? 16u : preset == kRgba16f ? 8u : 0u;
 }
@@ -29,6 +41,9 @@ struct DispatchParams {
   uint32_t inputLevel;  // L
   uint32_t levelCount;  // n
   uint64_t groups;      // reference workgroups covered (gx if gy, gz > 0, else 0)
+  // Format of the values handed through the reference's shared memory
+  // (sRGBA8 only): kSharedFp32, kSharedSrgb or kSharedF16.
+  uint32_t sharedFmt;
   LevelView lv[kMaxDispatchLevels + 1];
   // Strided batches (portable kernels only): `batch` images, image i's level
   // L+k at lv[k].ptr + i * imageStride[k].

@@ -38,11 +38,14 @@ __device__ __forceinline__ bool gridBarrier(const ChainParams& p, uint32_t& gen,
   return gridBarrierWait(p.barrierCount, p.barrierGen, p.errorFlag, gen, okFlag);
 }
 
+template <uint32_t SF>
 __device__ __forceinline__ void runStage(const Stage& st, uint32_t lane, uint32_t warpId, uint32_t warps, const Lut& L) {
   const uint32_t units = st.tilesX * st.bands;
-  for (uint32_t u = warpId; u < units; u += warps) strip(st, u % st.tilesX, u / st.tilesX, lane, L);
+  for (uint32_t u = warpId; u < units; u += warps) strip<SF>(st, u % st.tilesX, u / st.tilesX, lane, L);
 }
 
+// SF: the general pipeline's shared format (one per launch).
+template <uint32_t SF>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const __grid_constant__ ChainParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint32_t okFlag;
@@ -56,7 +59,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
 #pragma unroll 1
   for (uint32_t s = 0; s < p.stageCount; ++s) {
     const bool alone = s >= p.tailFrom;  // a small stage: this CTA alone
-    runStage(p.st[s], lane, alone ? localWarp : warpId, alone ? kWarps : warps, L);
+    runStage<SF>(p.st[s], lane, alone ? localWarp : warpId, alone ? kWarps : warps, L);
     if (s + 1 == p.stageCount) break;
     if (s + 1 < p.tailFrom) {
       if (!gridBarrier(p, gen, &okFlag)) return;
@@ -73,6 +76,12 @@ struct DeviceState {
   int ctasPerSm = 0;
 };
 
+const void* chainKernel(uint32_t sharedFmt) {
+  return sharedFmt == kSharedSrgb  ? reinterpret_cast<const void*>(generalChainKernel<kSharedSrgb>)
+         : sharedFmt == kSharedF16 ? reinterpret_cast<const void*>(generalChainKernel<kSharedF16>)
+                                   : reinterpret_cast<const void*>(generalChainKernel<kSharedFp32>);
+}
+
 cudaError_t deviceState(int* sms, int* ctasPerSm) {
   static DeviceState states[64];
   static std::mutex mu;
@@ -87,10 +96,12 @@ cudaError_t deviceState(int* sms, int* ctasPerSm) {
     e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (e != cudaSuccess) return e;
     if (!coop) return cudaErrorNotSupported;
-    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(generalChainKernel),
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.ctasPerSm, generalChainKernel, kThreads, kSmemBytes);
+    for (const void* k : {chainKernel(kSharedFp32), chainKernel(kSharedSrgb), chainKernel(kSharedF16)}) {
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
+      if (e != cudaSuccess) return e;
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.ctasPerSm, generalChainKernel<kSharedFp32>, kThreads,
+                                                      kSmemBytes);
     if (e != cudaSuccess) return e;
     if (d.ctasPerSm < 1) return cudaErrorInvalidConfiguration;
     e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
@@ -128,6 +139,8 @@ cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStre
                                uint32_t* launches) {
   if (count == 0 || count > kMaxStages || (count > 1 && scratch.counterCount <= kCounterBarrierGen))
     return cudaErrorInvalidValue;
+  for (uint32_t i = 1; i < count; ++i)
+    if (p[i].sharedFmt != p[0].sharedFmt) return cudaErrorInvalidValue;  // one shared format per launch
   int sms = 0, ctasPerSm = 0;
   cudaError_t e = deviceState(&sms, &ctasPerSm);
   if (e != cudaSuccess) return e;
@@ -154,8 +167,7 @@ cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStre
   uint32_t grid = count > 1 ? ctas : uint32_t(std::min<uint64_t>((maxUnits + kWarps - 1) / kWarps, ctas));
   if (cp.tailFrom == 0) grid = 1;
   void* args[] = {&cp};
-  e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(generalChainKernel), dim3(grid), dim3(kThreads),
-                                  args, kSmemBytes, stream);
+  e = cudaLaunchCooperativeKernel(chainKernel(p[0].sharedFmt), dim3(grid), dim3(kThreads), args, kSmemBytes, stream);
   if (e != cudaSuccess) return e;
   ++*launches;
   return cudaSuccess;

@@ -8,7 +8,8 @@
 // n levels reduces each 2^n x 2^n tile of level L with 2x2 box filters whose
 // operand order is fastVerticalFirst(n, k); a general dispatch of 1 or 2 levels
 // applies the 1..3-tap energy-conserving kernel.  Values stay FP32 inside a
-// dispatch and are quantised only by the STORE of each level.
+// dispatch and are quantised only by the STORE of each level, except the
+// hand-off level of a pipeline with a shared-memory format (handOff).
 #include <algorithm>
 
 #include "device_common.cuh"
@@ -36,6 +37,19 @@ __device__ __forceinline__ TexelIO<P> makeIO(SrgbTablesSmem* t) {
   TexelIO<P> io;
   io.t = t;
   return io;
+}
+
+// The value a dispatch hands on to its next level through the reference's
+// shared memory, in the pipeline's shared format `fmt` (sRGBA8 only;
+// srgba8_mipmap_preamble.glsl:60-108): the texel's code decoded again, or
+// each channel as binary16.  The hand-off level itself is stored from v.
+template <uint32_t P>
+__device__ __forceinline__ float4 handOff(uint32_t fmt, float4 v, const TexelIO<P>& io) {
+  if constexpr (P == kSrgba8) {
+    if (fmt == kSharedSrgb) return io.decode(io.encode(v));
+    if (fmt == kSharedF16) return f16RoundTrip(v);
+  }
+  return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -91,6 +105,7 @@ __global__ void __launch_bounds__(kThreads) portableFastKernel(DispatchParams p)
   float4* cur = bufA;
   float4* nxt = bufB;
   uint32_t curStride = 32;
+  const uint32_t handoffLevel = p.sharedFmt != kSharedFp32 ? sharedHandoffLevel(true, n) : 0u;
   for (uint32_t k = 2; k <= n; ++k) {
     const bool vert = fastVerticalFirst(n, k);
     const uint32_t nw = ew / 2, nh = eh / 2;
@@ -100,7 +115,7 @@ __global__ void __launch_bounds__(kThreads) portableFastKernel(DispatchParams p)
       const float4 tl = cur[(2 * y) * curStride + 2 * x], tr = cur[(2 * y) * curStride + 2 * x + 1];
       const float4 bl = cur[(2 * y + 1) * curStride + 2 * x], br = cur[(2 * y + 1) * curStride + 2 * x + 1];
       const float4 v = fastReduce(vert, tl, tr, bl, br);
-      nxt[y * nStride + x] = v;
+      nxt[y * nStride + x] = k == handoffLevel ? handOff<P>(p.sharedFmt, v, io) : v;
       if (covered(x0 + (x << k), y0 + (y << k)))
         io.store(texelAddr(levelOf(p, k), (x0 >> k) + x, (y0 >> k) + y, B), v);
     }
@@ -217,7 +232,7 @@ __global__ void __launch_bounds__(kThreads) portableGeneral2Kernel(DispatchParam
     const uint32_t x = wx0 + wx, y = wy0 + wy;
     auto ld = [&](uint32_t dx, uint32_t dy) { return io.load(texelAddr(l0, 2 * x + dx, 2 * y + dy, B)); };
     const float4 v = reduceSample(ld, kx, ky, l1.w, l1.h, x, y);
-    win[wy * kG2Win + wx] = v;
+    win[wy * kG2Win + wx] = handOff<P>(p.sharedFmt, v, io);
     const bool owner = min(x / (2 * kG2Tile), tilesX - 1) == tx && min(y / (2 * kG2Tile), tilesY - 1) == ty;
     if (owner && (full || g2CoveredL1(x, y, refWinW, refWinH, rtilesX, rtilesY, p.groups)))
       io.store(texelAddr(l1, x, y, B), v);

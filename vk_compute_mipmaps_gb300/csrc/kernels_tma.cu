@@ -189,8 +189,10 @@ __device__ __forceinline__ void levels12(const FusedStage& st, uint32_t x0, uint
 // cx % 4 == 0) from the level-(L+2) values, encoded in one pass: the
 // level-(L+4) value moves to the idle odd lane cx + 1, and each lane makes
 // at most one store.  For N >= 5 the level-(L+4) values go to `xchg`
-// ([row][col], 4x4).
-template <uint32_t N, bool CHECK>
+// ([row][col], 4x4).  SF: the pipeline's shared format, applied to the
+// values handed on from level L+3 (N = 4, 5) or L+4 (N = 6); the level
+// itself is stored from its FP32 values.
+template <uint32_t N, uint32_t SF, bool CHECK>
 __device__ __forceinline__ void levels34(const FusedStage& st, uint32_t x0, uint32_t y0, float4 c0, float4 c1,
                                          float4* xchg, uint32_t wig, uint32_t lane, const Lut& L) {
   if (N < 3) return;
@@ -202,10 +204,11 @@ __device__ __forceinline__ void levels34(const FusedStage& st, uint32_t x0, uint
   uint32_t k = 3, x = (x0 >> 3) + (cx >> 1), y = (y0 >> 3) + 2 * wig + half;
   bool store = (cx & 1) == 0;
   if (N >= 4) {
-    const float4 e = shflXor(d, 16);
-    const float4 dr = shflDown(d, 2), er = shflDown(e, 2);
-    const float4 f = fastReduceP(fastVerticalFirst(N, 4), d, dr, e, er);
-    if (N >= 5 && half == 0 && (cx & 3) == 0) xchg[wig * 4 + (cx >> 2)] = f;
+    const float4 dh = N <= 5 ? sharedRoundTrip<SF>(d, L) : d;
+    const float4 e = shflXor(dh, 16);
+    const float4 dr = shflDown(dh, 2), er = shflDown(e, 2);
+    const float4 f = fastReduceP(fastVerticalFirst(N, 4), dh, dr, e, er);
+    if (N >= 5 && half == 0 && (cx & 3) == 0) xchg[wig * 4 + (cx >> 2)] = N == 6 ? sharedRoundTrip<SF>(f, L) : f;
     const float4 fu = shflUp(f, 1);
     if (cx & 1) {
       v = fu;
@@ -275,7 +278,7 @@ __device__ __forceinline__ GroupCtx groupCtx(uint32_t g) {
 }
 
 // One region of the main (TMA-fed) loop for a consumer warp.
-template <uint32_t N, bool CHECK>
+template <uint32_t N, uint32_t SF, bool CHECK>
 __device__ __forceinline__ bool mainRegion(const FusedStage& st, const GroupCtx& G, uint32_t x0, uint32_t y0,
                                            uint32_t iter, uint32_t wig, uint32_t lane, const Lut& L) {
   const uint32_t s = iter & 1, ring = iter & 1;
@@ -287,7 +290,7 @@ __device__ __forceinline__ bool mainRegion(const FusedStage& st, const GroupCtx&
   // before depositing into this exchange slot again, the producer must have
   // finished the region that used it two steps ago
   if (N >= 5 && iter >= 2 && !mbarWait(G.xempty0 + 8 * ring, ((iter >> 1) - 1) & 1)) return false;
-  levels34<N, CHECK>(st, x0, y0, c0, c1, G.xchg + ring * 16, wig, lane, L);
+  levels34<N, SF, CHECK>(st, x0, y0, c0, c1, G.xchg + ring * 16, wig, lane, L);
   if (N >= 5) {
     __syncwarp();
     if (lane == 0) mbarArrive(G.xfull0 + 8 * ring);  // its part of the 4x4 block is deposited
@@ -311,7 +314,7 @@ struct RegionCursor {
   }
 };
 
-template <uint32_t N>
+template <uint32_t N, uint32_t SF>
 __device__ __forceinline__ bool consumerLoop(const FusedStage& st, const GroupCtx& G, uint32_t gid,
                                              uint32_t groupsTotal, uint32_t wig, uint32_t lane, const Lut& L) {
   RegionCursor c(gid, groupsTotal, st.regionsX);
@@ -320,12 +323,17 @@ __device__ __forceinline__ bool consumerLoop(const FusedStage& st, const GroupCt
     if (!mbarWait(G.full0 + 8 * s, (iter >> 1) & 1)) return false;
     const uint32_t x0 = c.rx * kTile, y0 = c.ry * kTile;
     const bool ok = (x0 + kTile > st.coverW || y0 + kTile > st.coverH)
-                        ? mainRegion<N, true>(st, G, x0, y0, iter, wig, lane, L)
-                        : mainRegion<N, false>(st, G, x0, y0, iter, wig, lane, L);
+                        ? mainRegion<N, SF, true>(st, G, x0, y0, iter, wig, lane, L)
+                        : mainRegion<N, SF, false>(st, G, x0, y0, iter, wig, lane, L);
     if (!ok) return false;
   }
   return true;
 }
+
+// The shared format that applies to an N-level dispatch of a pipeline with
+// format SF: only dispatches of 4 or more levels hand values on.
+template <uint32_t N, uint32_t SF>
+constexpr uint32_t kFmtOf = N >= 4 ? SF : kSharedFp32;
 
 // The producer warp of group g: refill region i's buffer with region i+2 as
 // soon as it is empty, then finish levels L+5/L+6 of region i.
@@ -357,6 +365,7 @@ __device__ __forceinline__ bool producerLoop(const FusedStage& st, const CUtenso
   return true;
 }
 
+template <uint32_t SF>
 __device__ __forceinline__ bool mainLoopN(const FusedStage& st, const CUtensorMap* map, uint32_t warp,
                                           uint32_t groupsTotal, uint32_t lane, const Lut& L) {
   if (warp >= kProducerWarp0) {
@@ -376,39 +385,40 @@ __device__ __forceinline__ bool mainLoopN(const FusedStage& st, const CUtensorMa
   const GroupCtx G = groupCtx(g);
   const uint32_t gid = g * gridDim.x + blockIdx.x;
   switch (st.n) {
-    case 1: return consumerLoop<1>(st, G, gid, groupsTotal, wig, lane, L);
-    case 2: return consumerLoop<2>(st, G, gid, groupsTotal, wig, lane, L);
-    case 3: return consumerLoop<3>(st, G, gid, groupsTotal, wig, lane, L);
-    case 4: return consumerLoop<4>(st, G, gid, groupsTotal, wig, lane, L);
-    case 5: return consumerLoop<5>(st, G, gid, groupsTotal, wig, lane, L);
-    default: return consumerLoop<6>(st, G, gid, groupsTotal, wig, lane, L);
+    case 1: return consumerLoop<1, kFmtOf<1, SF>>(st, G, gid, groupsTotal, wig, lane, L);
+    case 2: return consumerLoop<2, kFmtOf<2, SF>>(st, G, gid, groupsTotal, wig, lane, L);
+    case 3: return consumerLoop<3, kFmtOf<3, SF>>(st, G, gid, groupsTotal, wig, lane, L);
+    case 4: return consumerLoop<4, kFmtOf<4, SF>>(st, G, gid, groupsTotal, wig, lane, L);
+    case 5: return consumerLoop<5, kFmtOf<5, SF>>(st, G, gid, groupsTotal, wig, lane, L);
+    default: return consumerLoop<6, kFmtOf<6, SF>>(st, G, gid, groupsTotal, wig, lane, L);
   }
 }
 
 // One region of a tail dispatch: buffer filled with plain loads, group
 // barriers around the shared steps (the tail is a few regions at most).
-template <uint32_t N>
+template <uint32_t N, uint32_t SF>
 __device__ __forceinline__ void tailRegion(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
                                            float4* xchg, uint32_t g, uint32_t wig, uint32_t lane, uint32_t it,
                                            const Lut& L) {
   // the tail is a few regions: always bounds-checked
   float4 c0 = make_float4(0, 0, 0, 0), c1 = c0;
   levels12<N, true>(st, x0, y0, tile, wig, lane, L, c0, c1);
-  levels34<N, true>(st, x0, y0, c0, c1, xchg, wig, lane, L);
+  levels34<N, SF, true>(st, x0, y0, c0, c1, xchg, wig, lane, L);
   groupSync(g);
   if (N >= 5 && wig == (it & 3)) finishTop<N, true>(st, x0, y0, xchg, lane, L);
 }
 
+template <uint32_t SF>
 __device__ __forceinline__ void tailRegionN(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
                                             float4* xchg, uint32_t g, uint32_t wig, uint32_t lane, uint32_t it,
                                             const Lut& L) {
   switch (st.n) {
-    case 1: tailRegion<1>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 2: tailRegion<2>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 3: tailRegion<3>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 4: tailRegion<4>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 5: tailRegion<5>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    default: tailRegion<6>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 1: tailRegion<1, kFmtOf<1, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 2: tailRegion<2, kFmtOf<2, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 3: tailRegion<3, kFmtOf<3, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 4: tailRegion<4, kFmtOf<4, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    case 5: tailRegion<5, kFmtOf<5, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
+    default: tailRegion<6, kFmtOf<6, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
   }
 }
 
@@ -427,6 +437,8 @@ __device__ __forceinline__ void loadRegionPlain(const FusedStage& st, uint32_t x
   }
 }
 
+// SF: the fast pipeline's shared format (the same for every stage of a launch).
+template <uint32_t SF>
 __global__ void __launch_bounds__(kThreads, 1)
     tmaFastKernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TmaParams p) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -465,7 +477,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   }
   __syncwarp();
-  const bool ok = mainLoopN(s0, &tmap, warp, groupsTotal, lane, L);
+  const bool ok = mainLoopN<SF>(s0, &tmap, warp, groupsTotal, lane, L);
   if (!ok && lane == 0) {
     // A bounded wait gave up: record it and give the loads that may still be
     // in flight one more bounded wait before the CTA may exit.
@@ -499,7 +511,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t x0 = (r % st.regionsX) * kTile, y0 = (r / st.regionsX) * kTile;
       loadRegionPlain(st, x0, y0, tile, gtid);
       groupSync(g);
-      tailRegionN(st, x0, y0, tile, G.xchg + (it % kXchgRing) * 16, g, wig, lane, it, L);
+      tailRegionN<SF>(st, x0, y0, tile, G.xchg + (it % kXchgRing) * 16, g, wig, lane, it, L);
       groupSync(g);
     }
     // consumer warps only (the producer warps have left)
@@ -567,6 +579,12 @@ struct DeviceInfo {
   bool configured = false;
 };
 
+const void* tmaKernel(uint32_t sharedFmt) {
+  return sharedFmt == kSharedSrgb  ? reinterpret_cast<const void*>(tmaFastKernel<kSharedSrgb>)
+         : sharedFmt == kSharedF16 ? reinterpret_cast<const void*>(tmaFastKernel<kSharedF16>)
+                                   : reinterpret_cast<const void*>(tmaFastKernel<kSharedFp32>);
+}
+
 cudaError_t deviceInfo(DeviceInfo** out) {
   static DeviceInfo infos[64];
   static std::mutex mu;
@@ -578,8 +596,8 @@ cudaError_t deviceInfo(DeviceInfo** out) {
   DeviceInfo& d = infos[dev];
   if (!d.configured) {
     e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(tmaFastKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
+    for (const void* k : {tmaKernel(kSharedFp32), tmaKernel(kSharedSrgb), tmaKernel(kSharedF16)})
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(debugEncodeKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(kDebugSmemBytes));
@@ -628,7 +646,7 @@ bool tmaFastSupported(const DispatchParams& p) {
 
 bool tmaTailCompatible(const DispatchParams& prev, const DispatchParams& next) {
   if (next.preset != kSrgba8 || !next.isFast || next.levelCount < 1 || next.levelCount > 6) return false;
-  if (next.inputLevel != prev.inputLevel + prev.levelCount) return false;
+  if (next.inputLevel != prev.inputLevel + prev.levelCount || next.sharedFmt != prev.sharedFmt) return false;
   if (next.lv[0].ptr != prev.lv[prev.levelCount].ptr || next.lv[0].pitch != prev.lv[prev.levelCount].pitch)
     return false;
   if ((next.lv[0].w >> next.levelCount) == 0 || (next.lv[0].h >> next.levelCount) == 0) return false;
@@ -650,6 +668,8 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
   cudaError_t e = deviceInfo(&info);
   if (e != cudaSuccess) return e;
   if (tailCount + 1 > kMaxFused || (tailCount && scratch.counterCount < 2)) return cudaErrorInvalidValue;
+  for (uint32_t i = 0; i < tailCount; ++i)
+    if (tail[i].sharedFmt != p.sharedFmt) return cudaErrorInvalidValue;  // one shared format per launch
   TmaParams tp{};
   fillStage(p, &tp.st[0]);
   for (uint32_t i = 0; i < tailCount; ++i) fillStage(tail[i], &tp.st[i + 1]);
@@ -668,7 +688,9 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
   if (cr != CUDA_SUCCESS) return cudaErrorInvalidValue;
   const uint64_t regions = uint64_t(tp.st[0].regionsX) * tp.st[0].regionsY;
   const uint32_t grid = uint32_t(std::min<uint64_t>(regions, uint64_t(info->sms)));
-  tmaFastKernel<<<grid, kThreads, kSmemBytes, stream>>>(map, tp);
+  void* args[] = {&map, &tp};
+  e = cudaLaunchKernel(tmaKernel(p.sharedFmt), dim3(grid), dim3(kThreads), args, kSmemBytes, stream);
+  if (e != cudaSuccess) return e;
   ++*launches;
   return cudaGetLastError();
 }

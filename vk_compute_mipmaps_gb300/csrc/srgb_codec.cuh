@@ -151,6 +151,17 @@ __device__ __forceinline__ uint32_t encodeTexel(float4 v, const Lut& L) {
   return __byte_perm(__byte_perm(r, g, 0x0040), __byte_perm(b, a, 0x0040), 0x5410);
 }
 
+// The value a dispatch hands on to its next level through the reference's
+// shared memory, in the pipeline's shared format SF
+// (srgba8_mipmap_preamble.glsl:60-108): FP32 unchanged; SRGB_SHARED the
+// texel's sRGBA8 code decoded again; F16_SHARED each channel as binary16.
+template <uint32_t SF>
+__device__ __forceinline__ float4 sharedRoundTrip(float4 v, const Lut& L) {
+  if (SF == kSharedSrgb) return decodeTexel(encodeTexel(v, L), L);
+  if (SF == kSharedF16) return f16RoundTrip(v);
+  return v;
+}
+
 // REDUCE4 on packed pairs: 0.25 * ((v00 + v01) + (v10 + v11)) per channel,
 // same operations and order as reduce4().
 __device__ __forceinline__ float4 add4p(float4 a, float4 b) {

@@ -44,14 +44,21 @@ def packed_offsets(width: int, height: int, levels: int, bytes_per_texel: int) -
 class Pipelines:
     """NvproPyramidPipelines of one preset (nvpro_pyramid_dispatch.hpp:29-35)."""
 
-    def __init__(self, preset: int = N.PRESET_SRGBA8, fast: bool = True):
+    def __init__(self, preset: int = N.PRESET_SRGBA8, fast: bool = True, general_config: int = 0,
+                 fast_config: int = 0):
+        """general_config / fast_config: NVPRO_PYRAMID_CONFIG_* bits of each
+        pipeline (CONFIG_SRGB_SHARED, CONFIG_F16_SHARED, CONFIG_NO_BILINEAR),
+        as the reference demo's per-pipeline config bits
+        (demo_app/pipeline_alternative.cpp:25-32)."""
         lib = N.load()
         self.preset = preset
         self._general = ctypes.c_void_p()
         self._fast = ctypes.c_void_p()
-        N.check(lib.nvproPyramidCreatePipeline(preset, 0, ctypes.byref(self._general)), "create general pipeline")
+        N.check(lib.nvproPyramidCreatePipelineEx(preset, 0, general_config, ctypes.byref(self._general)),
+                "create general pipeline")
         if fast:
-            N.check(lib.nvproPyramidCreatePipeline(preset, 1, ctypes.byref(self._fast)), "create fast pipeline")
+            N.check(lib.nvproPyramidCreatePipelineEx(preset, 1, fast_config, ctypes.byref(self._fast)),
+                    "create fast pipeline")
 
     @property
     def struct(self) -> N.NvproPyramidPipelines:
