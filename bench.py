@@ -384,6 +384,53 @@ def cpu_baseline_sample(threads: int, reps: int = 1):
     return us_per_16384, dt, f"{chains_4096} x 4096^2 chains on {threads} threads ({dt:.2f} s), scaled by bytes"
 
 
+def cpu_detail_sample(threads: int):
+    """The CPU figures beside the headline baseline: one 4096^2 chain on one
+    thread with the restated reference generator and with the oracle (shader
+    semantics, reference schedule), and the 256-image benchmark batch over
+    `threads` threads (one image per thread at a time, as the reference
+    benchmark hands out images)."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT / "tests"))
+    import _oracle as O
+    from vk_compute_mipmaps_gb300.workloads import batch_sizes
+    lib = O.orc()
+    base = np.random.default_rng(0).integers(0, 256, (4096, 4096, 4), dtype=np.uint8)
+    buf = O.packed_from_base(1, base)
+    t0 = time.perf_counter()
+    lib.orc_refcpu_srgba8(4096, 4096, buf.ctypes.data_as(O.POINTER(O.c_uint8)))
+    ref_1t = time.perf_counter() - t0
+    buf = O.packed_from_base(1, base)
+    t0 = time.perf_counter()
+    O.run(1, 4096, 4096, buf)
+    orc_1t = time.perf_counter() - t0
+    sizes = batch_sizes(256)
+    rng = np.random.default_rng(2024)
+    bufs = [O.packed_from_base(1, rng.integers(0, 256, (h, w, 4), dtype=np.uint8)) for w, h in sizes]
+    order = sorted(range(len(sizes)), key=lambda i: -sizes[i][0] * sizes[i][1])  # largest first
+    lock = threading.Lock()
+
+    def work():
+        while True:
+            with lock:
+                if not order:
+                    return
+                i = order.pop(0)
+            w, h = sizes[i]
+            lib.orc_refcpu_srgba8(w, h, bufs[i].ctypes.data_as(O.POINTER(O.c_uint8)))
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work) for _ in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    batch_s = time.perf_counter() - t0
+    return {"single_thread_us_per_4096_chain": round(ref_1t * 1e6, 1),
+            "oracle_single_thread_us_per_4096_chain": round(orc_1t * 1e6, 1),
+            "batch_256_images_per_s": round(len(sizes) / batch_s, 1), "batch_256_threads": threads}
+
+
 def run_ours(args, rank, world):
     import torch
     import vk_compute_mipmaps_gb300 as V
@@ -471,6 +518,7 @@ def run_ours(args, rank, world):
             us, dt, sample = cpu_baseline_sample(threads)
             cpu = {"value": round(us, 1), "unit": "us per 16384^2 chain", "cores": threads, "kind": "port",
                    "sample": sample}
+            cpu.update(cpu_detail_sample(threads))
 
     line = {
         "metric": f"srgba8_{w}x{h}_full_chain_us",

@@ -50,7 +50,8 @@ typedef enum NvproPyramidResult {
   NVPRO_PYRAMID_ERROR_UNSUPPORTED      = 4, /* preset / layout not supported by a kernel */
   NVPRO_PYRAMID_ERROR_CUDA             = 5, /* a CUDA runtime call failed */
   NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY    = 6,
-  NVPRO_PYRAMID_ERROR_TIMEOUT          = 7  /* a bounded device-side wait gave up */
+  NVPRO_PYRAMID_ERROR_TIMEOUT          = 7, /* a bounded device-side wait gave up */
+  NVPRO_PYRAMID_ERROR_IO               = 8  /* a file could not be read or written */
 } NvproPyramidResult;
 
 /* Static description of a result code. */
@@ -436,6 +437,30 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchGetInfo(NvproPyramidBatch 
 /* Wait for the device, then report NVPRO_PYRAMID_ERROR_TIMEOUT if a bounded
  * grid-barrier wait of a launch of this batch gave up since the last query. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchDeviceStatus(NvproPyramidBatch batch);
+
+/* ------------------------------------------------------------------------ */
+/* Debugging I/O of sRGBA8 levels in HOST memory (no CUDA call).             */
+/* ------------------------------------------------------------------------ */
+
+/* One level (RGBA8 rows rowPitchBytes apart; 0 = 4 * width) as an
+ * uncompressed 32-bit TGA file, top-left origin. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidWriteTga(const char* path, const void* rgba8, uint32_t width,
+                                                          uint32_t height, uint64_t rowPitchBytes);
+
+/* writeMipmapsTga (include/mipmap_storage.hpp:436-479): levelCount levels
+ * (0 = all) of a packed chain (nvproPyramidPackedLayout, 4 bytes per texel)
+ * to TGA files: level 0 to baseFilename, level k to baseFilename with ".k"
+ * inserted before its extension ("out.tga" -> "out.3.tga"). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidWriteLevelsTga(const char* baseFilename, const void* packed,
+                                                                uint32_t width, uint32_t height,
+                                                                uint32_t levelCount);
+
+/* Read a 24- or 32-bit true-colour TGA (uncompressed or RLE, either vertical
+ * origin) into top-left RGBA8 rows (alpha 255 for 24-bit files).  With
+ * rgba8 == NULL only *pWidth / *pHeight are set; else capacityBytes must be
+ * at least 4 * width * height. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidReadTga(const char* path, void* rgba8, uint64_t capacityBytes,
+                                                         uint32_t* pWidth, uint32_t* pHeight);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -1,4 +1,5 @@
 """pytest configuration: the `gpu` marker and shared fixtures."""
+import shutil
 import sys
 from pathlib import Path
 
@@ -28,3 +29,14 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     return torch.device("cuda:0")
+
+
+@pytest.fixture
+def repo_tmp(request):
+    """A scratch directory inside the repository (tests/.tmp/<test>), removed
+    afterwards."""
+    d = ROOT / "tests" / ".tmp" / request.node.name.replace("[", "_").replace("]", "")
+    shutil.rmtree(d, ignore_errors=True)
+    d.mkdir(parents=True)
+    yield d
+    shutil.rmtree(d, ignore_errors=True)

@@ -1,5 +1,6 @@
 """Host-side logic without a GPU: the bench's multi-rank helpers as two gloo
 ranks, the synthetic batch workload, and the adjoint workspace rule."""
+import ctypes
 import os
 import socket
 
@@ -78,3 +79,56 @@ def _workspace_rule(w, h, mips=0):
                                       (4095, 4094, 0), (1920, 1080, 0), (2052, 2052, 0), (640, 384, 4)])
 def test_adjoint_workspace_bytes(native, w, h, mips):
     assert native.nvproPyramidAdjointWorkspaceBytes(w, h, mips) == _workspace_rule(w, h, mips)
+
+
+def test_write_levels_tga_round_trip(native, repo_tmp):
+    """writeMipmapsTga naming (include/mipmap_storage.hpp:436-479) and TGA
+    contents, read back through nvproPyramidReadTga."""
+    import numpy as np
+
+    import _oracle as O
+    import vk_compute_mipmaps_gb300 as V
+    w, h = 37, 20
+    base = np.random.default_rng(3).integers(0, 256, (h, w, 4), dtype=np.uint8)
+    packed = O.pyramid(1, base)
+    levels = O.full_levels(w, h)
+    off = O.offsets(w, h, levels, 4)
+    for name, stem, ext in (("mips.tga", "mips.", ".tga"), ("noext", "noext", "")):
+        path = repo_tmp / name
+        assert native.nvproPyramidWriteLevelsTga(str(path).encode(), packed.ctypes.data, w, h, 0) == 0
+        for k in range(levels):
+            f = path if k == 0 else repo_tmp / f"{stem}{k}{ext}"
+            lw, lh = max(w >> k, 1), max(h >> k, 1)
+            raw = f.read_bytes()
+            assert len(raw) == 18 + lw * lh * 4
+            assert raw[2] == 2 and raw[16] == 32 and raw[17] == 0x28  # uncompressed, 32 bpp, top-left
+            want = packed[off[k]:off[k + 1]].reshape(lh, lw, 4)
+            assert np.array_equal(V.read_tga(str(f)), want), (name, k)
+    V.write_tga(str(repo_tmp / "one.tga"), base)
+    assert np.array_equal(V.read_tga(str(repo_tmp / "one.tga")), base)
+
+
+def test_read_tga_rle_bottom_up_24bit(native, repo_tmp):
+    import numpy as np
+
+    import vk_compute_mipmaps_gb300 as V
+    from vk_compute_mipmaps_gb300 import _native as N
+    # 3x2, type 10 (RLE), 24 bpp, bottom-left origin: bottom row = a run of
+    # three (10, 20, 30) pixels; top row = raw packet of three pixels
+    hdr = bytes([0, 0, 10] + [0] * 9 + [3, 0, 2, 0, 24, 0])
+    body = bytes([0x82, 30, 20, 10, 0x02, 3, 2, 1, 6, 5, 4, 9, 8, 7])
+    (repo_tmp / "rle.tga").write_bytes(hdr + body)
+    got = V.read_tga(str(repo_tmp / "rle.tga"))
+    want = np.array([[[1, 2, 3, 255], [4, 5, 6, 255], [7, 8, 9, 255]],
+                     [[10, 20, 30, 255]] * 3], np.uint8)
+    assert np.array_equal(got, want)
+    (repo_tmp / "cmap.tga").write_bytes(bytes([0, 1, 1] + [0] * 15))
+    w, h = ctypes.c_uint32(), ctypes.c_uint32()
+    assert native.nvproPyramidReadTga(str(repo_tmp / "cmap.tga").encode(), None, 0, ctypes.byref(w),
+                                      ctypes.byref(h)) == N.ERROR_UNSUPPORTED
+    assert native.nvproPyramidReadTga(str(repo_tmp / "missing.tga").encode(), None, 0, ctypes.byref(w),
+                                      ctypes.byref(h)) == N.ERROR_IO
+    (repo_tmp / "short.tga").write_bytes(hdr + body[:5])
+    buf = np.empty(24, np.uint8)
+    assert native.nvproPyramidReadTga(str(repo_tmp / "short.tga").encode(), buf.ctypes.data, 24, ctypes.byref(w),
+                                      ctypes.byref(h)) == N.ERROR_IO

@@ -22,6 +22,7 @@ ERROR_UNSUPPORTED = 4
 ERROR_CUDA = 5
 ERROR_OUT_OF_MEMORY = 6
 ERROR_TIMEOUT = 7
+ERROR_IO = 8
 
 PRESET_SRGBA8 = 1
 PRESET_RGBA32F = 2
@@ -105,6 +106,9 @@ SIGNATURES = {
     "nvproPyramidLastError": (c_char_p, []),
     "nvproPyramidCreatePipeline": (c_int, [c_int, c_uint32, POINTER(c_void_p)]),
     "nvproPyramidCreatePipelineEx": (c_int, [c_int, c_uint32, c_uint32, POINTER(c_void_p)]),
+    "nvproPyramidWriteTga": (c_int, [c_char_p, c_void_p, c_uint32, c_uint32, c_uint64]),
+    "nvproPyramidWriteLevelsTga": (c_int, [c_char_p, c_void_p, c_uint32, c_uint32, c_uint32]),
+    "nvproPyramidReadTga": (c_int, [c_char_p, c_void_p, c_uint64, POINTER(c_uint32), POINTER(c_uint32)]),
     "nvproPyramidDestroyPipeline": (None, [c_void_p]),
     "nvproPyramidPresetTexelBytes": (c_uint32, [c_int]),
     "nvproPyramidFullLevelCount": (c_uint32, [c_uint32, c_uint32]),

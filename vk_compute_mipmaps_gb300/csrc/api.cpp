@@ -158,11 +158,18 @@ const char* nvproPyramidResultString(NvproPyramidResult r) {
     case NVPRO_PYRAMID_ERROR_CUDA: return "CUDA error";
     case NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY: return "out of memory";
     case NVPRO_PYRAMID_ERROR_TIMEOUT: return "device wait timed out";
+    case NVPRO_PYRAMID_ERROR_IO: return "file I/O failed";
   }
   return "unknown result";
 }
 
 const char* nvproPyramidLastError(void) { return t_lastError.c_str(); }
+
+}  // extern "C"
+
+void nvpyr::setLastError(const char* text) { t_lastError = text; }
+
+extern "C" {
 
 uint32_t nvproPyramidPresetTexelBytes(NvproPyramidPreset preset) { return presetBytes(uint32_t(preset)); }
 

@@ -132,4 +132,7 @@ constexpr uint32_t kCounterBarrierGen = 3;  // general chain: barrier generation
 constexpr uint32_t kStaticScratchWords = 64;
 cudaError_t staticScratch(uint32_t** ptr);
 
+// Set the calling thread's nvproPyramidLastError text.
+void setLastError(const char* text);
+
 }  // namespace nvpyr

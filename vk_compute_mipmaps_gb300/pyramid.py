@@ -255,6 +255,41 @@ def generate(chain: MipChain, stream: Optional[int] = None, mip_levels: int = 0,
     return cmd.launch_count
 
 
+def write_levels_tga(chain: "MipChain", base_filename: str, levels: int = 0) -> None:
+    """Write the levels of an sRGBA8 chain to TGA files (level 0 to
+    base_filename, level k to base_filename with ".k" before the extension),
+    as the reference's writeMipmapsTga does.  Copies the chain to the host."""
+    import numpy as np
+    if chain.preset != N.PRESET_SRGBA8:
+        raise ValueError("TGA output exists for the sRGBA8 preset only")
+    host = np.ascontiguousarray(chain.storage.cpu().numpy())
+    N.check(N.load().nvproPyramidWriteLevelsTga(str(base_filename).encode(), host.ctypes.data, chain.width,
+                                                 chain.height, levels or chain.levels), "write levels")
+
+
+def read_tga(path: str):
+    """A 24/32-bit TGA file as a [h, w, 4] uint8 numpy array (RGBA, top row first)."""
+    import numpy as np
+    lib = N.load()
+    w, h = ctypes.c_uint32(), ctypes.c_uint32()
+    N.check(lib.nvproPyramidReadTga(str(path).encode(), None, 0, ctypes.byref(w), ctypes.byref(h)), "read TGA")
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    N.check(lib.nvproPyramidReadTga(str(path).encode(), out.ctypes.data, out.nbytes, ctypes.byref(w),
+                                    ctypes.byref(h)), "read TGA")
+    return out
+
+
+def write_tga(path: str, rgba) -> None:
+    """Write a [h, w, 4] uint8 array (numpy or a CPU/CUDA tensor) as a TGA file."""
+    import numpy as np
+    a = rgba.cpu().numpy() if hasattr(rgba, "cpu") else rgba
+    a = np.ascontiguousarray(a, dtype=np.uint8)
+    if a.ndim != 3 or a.shape[2] != 4:
+        raise ValueError("expected [h, w, 4] uint8")
+    N.check(N.load().nvproPyramidWriteTga(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0], 0),
+            "write TGA")
+
+
 _copy_streams_cache: dict = {}
 
 
