@@ -202,6 +202,24 @@ def bench_config(w, h, dev, stream, flush, steps, content="random"):
     return out
 
 
+def bench_premultiply(dev, stream, steps, w=16384, h=16384):
+    """The premultiplied-alpha staging pass over a 16384^2 sRGBA8 image in
+    place (1 GiB read + 1 GiB written; larger than L2), device-timed."""
+    import torch
+    import vk_compute_mipmaps_gb300 as V
+    g = torch.Generator(device=dev).manual_seed(77)
+    img = torch.randint(0, 256, (h, w, 4), generator=g, device=dev, dtype=torch.uint8)
+    with torch.cuda.stream(stream):
+        ts = time_loop(lambda: V.premultiply_alpha(img, stream=stream.cuda_stream), stream, steps, 3)
+    us = statistics.median(ts) * 1e3
+    nbytes = 2 * w * h * 4
+    peak, _ = measured_peak()
+    del img
+    torch.cuda.empty_cache()
+    return {"image": f"{w}x{h}", "us": round(us, 1), "GBps": round(nbytes / (us * 1e-6) / 1e9, 1),
+            "frac_of_hbm_peak": round(nbytes / (us * 1e-6) / 1e9 / peak, 4), "bytes": nbytes}
+
+
 def bench_batch(dev, stream, flush, steps):
     """256 sRGBA8 images (sides log-uniform in [17, 4096], aspect in [1/4, 4],
     seed 2024) in one buffer: one batch launch (autotuned, CUDA graph) against
@@ -481,6 +499,17 @@ def run_ours(args, rank, world):
     extra = {"chain_GBps": round(chain_bytes / (ms_per_step * 1e-3) / 1e9, 1),
              "chain_frac_of_hbm_peak": round(chain_bytes / (ms_per_step * 1e-3) / 1e9 / peak, 4),
              "chain_algorithmic_bytes": chain_bytes, "launches_per_chain": launches_per_chain}
+    # Speed-of-light probe: one launch with the chain's traffic and no
+    # filtering (levels 1.. get non-pyramid values; the base is untouched).
+    img = chain.image()
+    probe = lambda: V._native.check(  # noqa: E731
+        V._native.load().nvproPyramidSpeedOfLightProbe(stream.cuda_stream, ctypes.byref(img), 0), "probe")
+    with torch.cuda.stream(stream):
+        pt = time_loop(probe, stream, max(20, min(args.steps, 200)), 3)
+    probe_us = statistics.mean(pt) * 1e3
+    extra["speed_of_light_probe"] = {
+        "us": round(probe_us, 2), "frac_of_hbm_peak": round(chain_bytes / (probe_us * 1e-6) / 1e9 / peak, 4),
+        "chain_over_probe": round(us_per_chain / probe_us, 3)}
     e2e = None
     cpu = None
     if rank == 0 and not args.no_e2e:
@@ -511,6 +540,7 @@ def run_ours(args, rank, world):
                                                    content)
                 extra[f"{cw}x{ch}"]["content"] = content
             extra["batch_256"] = bench_batch(dev, stream, flush, max(5, min(args.steps, 20)))
+            extra["premultiply_staging"] = bench_premultiply(dev, stream, max(5, min(args.steps, 20)))
             extra["float_adjoint"] = bench_float_adjoint(dev, stream, flush, max(5, min(args.steps, 20)))
             del flush
         if not args.no_cpu:
@@ -623,6 +653,13 @@ def run_profile(spec: str, reps: int):
         ups = [torch.randn((1, lh, lw, 4), generator=g, device=dev).to(dt) for lw, lh in level_sizes(w, h)]
         for _ in range(reps):
             A.adjoint(ups, (1, h, w, 4), dt, dev)
+        torch.cuda.synchronize()
+    elif spec.startswith("premultiply:"):
+        w, h = map(int, spec.split(":")[1].lower().split("x"))
+        img = torch.randint(0, 256, (h, w, 4), generator=torch.Generator(device=dev).manual_seed(77), device=dev,
+                            dtype=torch.uint8)
+        for _ in range(reps):
+            V.premultiply_alpha(img)
         torch.cuda.synchronize()
     else:
         raise SystemExit(f"unknown --profile workload {spec!r}")

@@ -234,6 +234,26 @@ NVPRO_PYRAMID_API uint32_t nvproPyramidCmdLaunchCount(NvproPyramidCmd cmd);
  * No reference counterpart: Vulkan reports device loss instead. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd cmd);
 
+/* Speed-of-light probe (the reference's "baseline" general-pipeline
+ * alternative, extras/general_pipelines/baseline/
+ * general_pipeline_alternative.glsl:1-26): one launch with the memory traffic
+ * of a whole sRGBA8 chain (level 0 read once, levels 1 .. mipLevels-1 written
+ * once) and no filtering, as a roofline calibration.  The levels it writes
+ * are NOT a pyramid.  Image >= 2x2; mipLevels 0 = all. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidSpeedOfLightProbe(
+    NvproPyramidStream stream, const NvproPyramidImage* pImage, uint32_t mipLevels);
+
+/* Premultiplied-alpha staging (the -do-premultiply-alpha path of
+ * minimal_app/minimal_mipmaps.cpp:316-367, done by the reference on the host
+ * in include/scoped_image.hpp:233-255): every sRGBA8 texel of a width x height
+ * image in DEVICE memory becomes (enc(dec(r) * a), enc(dec(g) * a),
+ * enc(dec(b) * a), A) with a = A * (1.0f / 255.0f) in FP32, dec the exact sRGB
+ * decode and enc the exact sRGB encode of the pyramid kernels.  src == dst
+ * (in place) is allowed; pitches 0 mean 4 * width.  Asynchronous on stream. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidPremultiplyAlpha(
+    NvproPyramidStream stream, const void* src, uint64_t srcPitch, void* dst, uint64_t dstPitch,
+    uint32_t width, uint32_t height);
+
 /* Test support (no reference counterpart): encode n floats of x (device
  * memory) with the kernels' fast sRGB encoder into `fast` (inputs clamped to
  * its domain [0, 1] first), and with the exact threshold count into `exact`. */

@@ -725,6 +725,28 @@ uint16_t orc_float_to_half(float f) { return floatToHalf(f); }
 float orc_ref_linear_from_srgb(uint32_t c) { return refLinearFromSrgb(c); }
 uint32_t orc_ref_srgb_from_linear(float x) { return refSrgbFromLinear(x); }
 
+// Premultiplied-alpha staging (include/scoped_image.hpp:233-255) of n sRGBA8
+// texels: a = A * (1.F / 255.F); colour c -> srgbFromLinear(linearFromSrgb(c)
+// * a); alpha unchanged.  referenceMath = 1: the reference's FP32 pow()
+// formulas (shaders/srgb.h, restated above); 0: the library's pinned exact
+// codec (decode table, threshold-count encode).
+void orc_premultiply_srgba8(const uint8_t* src, uint8_t* dst, uint64_t n, int referenceMath) {
+  const SrgbTables& t = tables();
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint8_t* s = src + 4 * i;
+    uint8_t* d = dst + 4 * i;
+    const float alpha = (float)s[3] * (1.F / 255.F);
+    uint8_t out[4];
+    for (int c = 0; c < 3; ++c) {
+      const float lin = referenceMath ? refLinearFromSrgb(s[c]) : t.decode[s[c]];
+      const float v = lin * alpha;
+      out[c] = (uint8_t)(referenceMath ? refSrgbFromLinear(v) : srgbEncode(v));
+    }
+    out[3] = s[3];
+    std::memcpy(d, out, 4);
+  }
+}
+
 // Encode an array of floats (for exhaustive comparisons).
 void orc_srgb_encode_array(const float* x, uint8_t* out, uint64_t n) {
   for (uint64_t i = 0; i < n; ++i) out[i] = (uint8_t)srgbEncode(x[i]);

@@ -43,6 +43,8 @@ def orc() -> ctypes.CDLL:
         lib.orc_alpha_encode.argtypes = [c_float]
         lib.orc_alpha_encode.restype = c_uint32
         lib.orc_srgb_encode_array.argtypes = [POINTER(c_float), POINTER(c_uint8), c_uint64]
+        lib.orc_premultiply_srgba8.argtypes = [POINTER(c_uint8), POINTER(c_uint8), c_uint64, c_int]
+        lib.orc_premultiply_srgba8.restype = None
         lib.orc_half_to_float.argtypes = [c_uint16]
         lib.orc_half_to_float.restype = c_float
         lib.orc_float_to_half.argtypes = [c_float]
@@ -186,3 +188,24 @@ def ref_events(lib, w, h, mips, has_fast, variant):
     n = lib.ref_dispatch_events(w, h, mips, int(has_fast), variant, buf, 1024)
     assert n >= 0
     return [tuple(buf[4 * i:4 * i + 4]) for i in range(n)]
+
+
+def premultiply(rgba: np.ndarray, reference_math: bool = False) -> np.ndarray:
+    """Premultiplied-alpha staging of uint8 RGBA texels (any shape [..., 4])."""
+    src = np.ascontiguousarray(rgba, np.uint8)
+    out = np.empty_like(src)
+    orc().orc_premultiply_srgba8(src.ctypes.data_as(POINTER(c_uint8)), out.ctypes.data_as(POINTER(c_uint8)),
+                                 src.size // 4, int(reference_math))
+    return out
+
+
+def all_code_alpha_pairs() -> np.ndarray:
+    """[256, 256, 4] uint8: texel (x=c, y=A) = (c, 255 - c, c ^ 0x5A, A): every
+    colour code with every alpha in each colour channel."""
+    c = np.arange(256, dtype=np.uint8)
+    img = np.empty((256, 256, 4), np.uint8)
+    img[..., 0] = c[None, :]
+    img[..., 1] = (255 - c)[None, :]
+    img[..., 2] = (c ^ 0x5A)[None, :]
+    img[..., 3] = c[:, None]
+    return img

@@ -9,8 +9,13 @@ code, compiled from its sources by `make -C oracle ref`:
   (nvpro_pyramid/nvpro_pyramid_dispatch.hpp) records for many image sizes,
   mip counts and dispatcher variants, captured through a recording stub of
   the Vulkan declarations it uses.
+* premultiply_all_pairs.json -- the SHA-256 of the premultiplied-alpha
+  staging (include/scoped_image.hpp:233-255: linearFromSrgb(c) *
+  (A * (1.F / 255.F)) -> srgbFromLinear, shaders/srgb.h from the reference
+  build) of the image holding every (colour code, alpha) pair in each
+  channel (_oracle.all_code_alpha_pairs).
 
-Run from the repository root: python tests/golden/make_golden.py
+Run from the repository root: python tests/golden/make_golden.py [premultiply]
 """
 from __future__ import annotations
 
@@ -38,11 +43,28 @@ def seed_of(w: int, h: int) -> int:
     return 1000003 * w + h
 
 
+def premultiply_golden(ref) -> None:
+    import hashlib
+    img = O.all_code_alpha_pairs()
+    alpha = img[..., 3].astype(np.float32) * np.float32(1.0 / 255.0)
+    out = img.copy()
+    lin = np.array([ref.ref_linear_from_srgb(c) for c in range(256)], np.float32)
+    for ch in range(3):
+        prod = (lin[img[..., ch]] * alpha).astype(np.float32)
+        out[..., ch] = np.array([ref.ref_srgb_from_linear(float(v)) for v in prod.reshape(-1)]).reshape(256, 256)
+    digest = hashlib.sha256(out.tobytes()).hexdigest()
+    (HERE / "premultiply_all_pairs.json").write_text(json.dumps({"sha256": digest, "shape": list(out.shape)}) + "\n")
+    print("premultiply golden", digest)
+
+
 def main() -> None:
     ref = O.ref_cpu()
     rd = O.ref_dispatch()
     if ref is None or rd is None:
         sys.exit("oracle/_ref is not built (make -C oracle ref needs the reference sources)")
+    premultiply_golden(ref)
+    if sys.argv[1:] == ["premultiply"]:
+        return
     vec = {}
     for w, h in REFCPU_SIZES:
         base = np.random.default_rng(seed_of(w, h)).integers(0, 256, (h, w, 4), dtype=np.uint8)

@@ -193,3 +193,14 @@ def test_pipeline_config_bits(native):
     cmd.end()
     recs = cmd.records()
     assert [(r["isFastPipeline"], r["configBits"]) for r in recs] == [(1, 2), (0, 1), (1, 2), (0, 1)]
+
+
+def test_premultiply_argument_checks(native):
+    # rejected before any CUDA call (the pointers are never dereferenced)
+    base = 0x7F0000000000
+    f = native.nvproPyramidPremultiplyAlpha
+    assert f(None, None, 0, base, 0, 8, 8) == N.ERROR_INVALID_ARGUMENT  # null source
+    assert f(None, base, 0, base, 0, 0, 8) == N.ERROR_INVALID_ARGUMENT  # empty
+    assert f(None, base, 16, base, 0, 8, 8) == N.ERROR_INVALID_ARGUMENT  # pitch below 4 * width
+    assert f(None, base + 2, 0, base + 2, 0, 8, 8) == N.ERROR_UNSUPPORTED  # texels not 4-byte aligned
+    assert f(None, base, 0, base + 64, 0, 8, 8) == N.ERROR_INVALID_ARGUMENT  # overlapping, not equal

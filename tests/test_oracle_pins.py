@@ -245,3 +245,17 @@ def test_srgb_shared_equals_split_dispatches(w, h, mips):
     got = O.pyramid(1, base, mips=mips, fast_shared=O.SHARED_SRGB, general_shared=O.SHARED_SRGB)
     want = O.pyramid(1, base, schedule=split_schedule(w, h, mips), mips=mips)
     assert np.array_equal(got, want)
+
+
+def test_premultiply_matches_reference_staging_golden():
+    # every (colour code, alpha) pair: the pinned codec and the restated
+    # reference formulas both give the bytes of the reference's own staging
+    # (hash recorded from the reference build by tests/golden/make_golden.py)
+    import hashlib
+    golden = json.loads((GOLDEN / "premultiply_all_pairs.json").read_text())["sha256"]
+    img = O.all_code_alpha_pairs()
+    assert hashlib.sha256(O.premultiply(img).tobytes()).hexdigest() == golden
+    assert hashlib.sha256(O.premultiply(img, reference_math=True).tobytes()).hexdigest() == golden
+    out = O.premultiply(img)
+    assert np.array_equal(out[..., 3], img[..., 3])  # alpha unchanged
+    assert np.array_equal(out[255], img[255]) and not out[0, :, :3].any()  # A = 255 keeps, A = 0 clears

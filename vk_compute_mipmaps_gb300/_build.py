@@ -16,7 +16,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libnvpro_pyramid_cuda.so"
 SOURCES = ["api.cpp", "host_io.cpp", "kernels_portable.cu", "kernels_tma.cu", "kernels_adjoint.cu",
-           "kernels_general.cu", "kernels_batch.cu"]
+           "kernels_general.cu", "kernels_batch.cu", "kernels_stage.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-I", str(PKG.parent / "include")]

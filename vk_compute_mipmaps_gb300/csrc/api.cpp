@@ -581,6 +581,50 @@ NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd cmd) {
   return NVPRO_PYRAMID_SUCCESS;
 }
 
+NvproPyramidResult nvproPyramidSpeedOfLightProbe(NvproPyramidStream stream, const NvproPyramidImage* pImage,
+                                                uint32_t mipLevels) {
+  if (!pImage) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pImage is NULL");
+  const uint32_t w = pImage->width, h = pImage->height;
+  const uint32_t full = nvproPyramidFullLevelCount(w, h);
+  if (mipLevels == 0) mipLevels = full;
+  if (w < 2 || h < 2 || mipLevels < 2 || mipLevels > full || pImage->levelCount < mipLevels)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "the probe needs a %ux%u image (>= 2x2) with %u levels bound", w,
+                h, mipLevels);
+  const uint8_t* levels[NVPRO_PYRAMID_MAX_LEVELS];
+  uint64_t pitches[NVPRO_PYRAMID_MAX_LEVELS];
+  for (uint32_t k = 0; k < mipLevels; ++k) {
+    levels[k] = static_cast<const uint8_t*>(pImage->levels[k]);
+    pitches[k] = pImage->rowPitchBytes[k] ? pImage->rowPitchBytes[k] : uint64_t(levelDim(w, k)) * 4;
+    if (!levels[k] || reinterpret_cast<uintptr_t>(levels[k]) % 4 || pitches[k] % 4)
+      return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "level %u: null or not 4-byte aligned", k);
+  }
+  const cudaError_t e = launchProbe(levels, pitches, w, h, mipLevels, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "probe launch failed: %s", cudaGetErrorString(e));
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidPremultiplyAlpha(NvproPyramidStream stream, const void* src, uint64_t srcPitch,
+                                               void* dst, uint64_t dstPitch, uint32_t width, uint32_t height) {
+  if (!src || !dst) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "null image");
+  if (width == 0 || height == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "zero width or height");
+  if (!srcPitch) srcPitch = uint64_t(width) * 4;
+  if (!dstPitch) dstPitch = uint64_t(width) * 4;
+  if (srcPitch < uint64_t(width) * 4 || dstPitch < uint64_t(width) * 4)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "row pitch below 4 * width");
+  if ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst) | srcPitch | dstPitch) % 4)
+    return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "texels must be 4-byte aligned");
+  if (src != dst && srcPitch == dstPitch) {  // overlapping but distinct images are not supported
+    const uintptr_t a = reinterpret_cast<uintptr_t>(src), b = reinterpret_cast<uintptr_t>(dst);
+    const uint64_t bytes = srcPitch * (height - 1) + uint64_t(width) * 4;
+    if (a < b + bytes && b < a + bytes)
+      return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "source and destination overlap without being equal");
+  }
+  const cudaError_t e = launchPremultiply(static_cast<const uint8_t*>(src), srcPitch, static_cast<uint8_t*>(dst),
+                                          dstPitch, width, height, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "premultiply launch failed: %s", cudaGetErrorString(e));
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
 NvproPyramidResult nvproPyramidDebugSrgbEncode(NvproPyramidStream stream, const float* x, uint8_t* fast,
                                                uint8_t* exact, uint64_t n) {
   if (!x || !fast || !exact) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "NULL buffer");

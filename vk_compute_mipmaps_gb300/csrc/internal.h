@@ -116,6 +116,14 @@ uint32_t generalMaxStages();
 cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStream_t stream, const Scratch& scratch,
                                uint32_t* launches);
 
+// Premultiplied-alpha staging of sRGBA8 texels (kernels_stage.cu); src may equal dst.
+cudaError_t launchPremultiply(const uint8_t* src, uint64_t srcPitch, uint8_t* dst, uint64_t dstPitch, uint32_t width,
+                              uint32_t height, cudaStream_t stream);
+
+// Speed-of-light probe (kernels_stage.cu): the traffic of a chain, no filtering.
+cudaError_t launchProbe(const uint8_t* const* levels, const uint64_t* pitches, uint32_t width, uint32_t height,
+                        uint32_t levelCount, cudaStream_t stream);
+
 cudaError_t launchAdjointChain(const AdjointChainParams& p, cudaStream_t stream);
 cudaError_t launchAdjointLevel(const AdjointLevelParams& p, cudaStream_t stream);
 

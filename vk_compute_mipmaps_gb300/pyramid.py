@@ -328,8 +328,30 @@ def _sub_image(chain: "MipChain", first: int, count: int, row0: int, rows: int) 
     return make_image(ptrs, sizes[first][0], rows, pitches)
 
 
+def premultiply_alpha(src, dst=None, stream: Optional[int] = None):
+    """Premultiplied-alpha staging of an sRGBA8 image on the GPU
+    (nvproPyramidPremultiplyAlpha): `src` is a CUDA uint8 tensor [h, w, 4]
+    (rows may be strided); the result goes to `dst` (same shape; default:
+    in place) and is returned."""
+    import torch
+    if src.dtype != torch.uint8 or src.dim() != 3 or src.shape[2] != 4 or not src.is_cuda:
+        raise ValueError("expected a CUDA uint8 tensor [h, w, 4]")
+    dst = src if dst is None else dst
+    if dst.shape != src.shape or dst.dtype != torch.uint8 or not dst.is_cuda:
+        raise ValueError("dst must match src")
+    for t in (src, dst):
+        if t.stride(2) != 1 or t.stride(1) != 4:
+            raise ValueError("texels of a row must be contiguous")
+    if stream is None:
+        stream = torch.cuda.current_stream(src.device).cuda_stream
+    h, w = src.shape[:2]
+    N.check(N.load().nvproPyramidPremultiplyAlpha(stream, src.data_ptr(), src.stride(0), dst.data_ptr(),
+                                                   dst.stride(0), w, h), "premultiply alpha")
+    return dst
+
+
 def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Optional[int] = None, bands: int = 8,
-                       flags: int = 0) -> None:
+                       flags: int = 0, premultiply: bool = False) -> None:
     """Level 0 from pinned host memory (`host_base`, chain.offsets[1] bytes),
     levels 1.. back to pinned host memory (`host_levels`, the rest of the
     packed chain), with the copies overlapped with the generation.
@@ -340,8 +362,11 @@ def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Option
     previous band's levels 1..n are copied out; the remaining dispatches run
     on level n after the last band.  The dispatches, and so the bytes, are
     those of `generate` on the whole chain.  Otherwise: copy in, generate,
-    copy out.  Returns when the work is queued; `stream` (default: torch's
-    current stream) waits for all of it."""
+    copy out.  With `premultiply` (sRGBA8), each band of level 0 is
+    premultiplied in place on the device right after its copy, as the
+    reference's -do-premultiply-alpha staging does before the pyramid (the
+    host copy of level 0 is left as it was).  Returns when the work is
+    queued; `stream` (default: torch's current stream) waits for all of it."""
     import torch
     dev = chain.storage.device
     cur = torch.cuda.current_stream(dev) if stream is None else torch.cuda.ExternalStream(stream, device=dev)
@@ -349,17 +374,29 @@ def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Option
     n = _first_fast_levels(chain.width, chain.height, chain.levels)
     rows_unit = 1 << n
     band_rows = -(-chain.height // max(bands, 1) // rows_unit) * rows_unit if n else chain.height
-    if not n or bands <= 1 or band_rows >= chain.height:
-        chain.storage[:off[1]].copy_(host_base, non_blocking=True)
-        generate(chain, stream=cur.cuda_stream, flags=flags)
-        host_levels.copy_(chain.storage[off[1]:off[-1]], non_blocking=True)
-        return
+    if premultiply and chain.preset != N.PRESET_SRGBA8:
+        raise ValueError("premultiplied alpha is an sRGBA8 staging step")
     lib = N.load()
+    pitch0 = chain.width * chain.bpp
+
+    def premultiply_rows(r0, rows):
+        ptr = chain.storage.data_ptr() + r0 * pitch0
+        N.check(lib.nvproPyramidPremultiplyAlpha(cur.cuda_stream, ptr, pitch0, ptr, pitch0, chain.width, rows),
+                "premultiply alpha")
+
+    if not n or bands <= 1 or band_rows >= chain.height:
+        with torch.cuda.stream(cur):
+            chain.storage[:off[1]].copy_(host_base, non_blocking=True)
+        if premultiply:
+            premultiply_rows(0, chain.height)
+        generate(chain, stream=cur.cuda_stream, flags=flags)
+        with torch.cuda.stream(cur):
+            host_levels.copy_(chain.storage[off[1]:off[-1]], non_blocking=True)
+        return
     p, c = _defaults(chain.preset, flags)
     copy_in, copy_out = _copy_streams(dev)
     copy_in.wait_stream(cur)
     copy_out.wait_stream(cur)
-    pitch0 = chain.width * chain.bpp
     sizes = level_sizes(chain.width, chain.height, chain.levels)
     r0 = 0
     while r0 < chain.height:
@@ -368,6 +405,8 @@ def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Option
         with torch.cuda.stream(copy_in):
             chain.storage[a:b].copy_(host_base[a:b], non_blocking=True)
         cur.wait_stream(copy_in)
+        if premultiply:
+            premultiply_rows(r0, rows)
         img = _sub_image(chain, 0, n + 1, r0, rows)
         N.check(lib.nvproPyramidGenerate(c.handle, cur.cuda_stream, p.struct, ctypes.byref(img), n + 1),
                 "nvproPyramidGenerate")
