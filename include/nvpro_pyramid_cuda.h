@@ -206,6 +206,18 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdPushConstants(
  * a smaller count leaves the reference's uncovered texels unwritten. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdDispatch(
     NvproPyramidCmd cmd, uint32_t groupCountX, uint32_t groupCountY, uint32_t groupCountZ);
+/* vkCmdBlitImage of level srcLevel to level srcLevel + 1 of the bound image
+ * with VK_FILTER_LINEAR (the fallback of the demo's "generalblit" mode,
+ * demo_app/mipmap_pipelines.cpp:350-452), in the texel format of the bound
+ * pipeline's preset.  Destination texel (x, y) samples the source at
+ * ((x + 0.5) * srcW / dstW, (y + 0.5) * srcH / dstH) with a bilinear filter
+ * on decoded (linear) values, clamped to the edge, and is stored with the
+ * preset's encoding.  The blit's filter precision is the Vulkan
+ * implementation's; here it is FP32, each operation rounded: scale =
+ * srcW / dstW, u = (x + 0.5) * scale - 0.5, i = floor(u), a = u - i;
+ * rows lerped first (t0 * (1 - a) + t1 * a), then the column. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdBlitLevel(NvproPyramidCmd cmd, uint32_t srcLevel);
+
 /* vkCmdPipelineBarrier (nvpro_pyramid_dispatch.hpp:183-186). */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCmdPipelineBarrier(NvproPyramidCmd cmd);
 
@@ -220,6 +232,7 @@ typedef struct NvproPyramidDispatchRecord {
   uint32_t pipelineBound;  /* a bind preceded this dispatch */
   uint32_t barrierBefore;  /* a barrier preceded this dispatch */
   uint32_t configBits;     /* NVPRO_PYRAMID_CONFIG_* of the bound pipeline */
+  uint32_t isBlit;         /* a blit (nvproPyramidCmdBlitLevel), not a dispatch */
 } NvproPyramidDispatchRecord;
 
 NVPRO_PYRAMID_API uint32_t nvproPyramidCmdRecordCount(NvproPyramidCmd cmd);
@@ -318,6 +331,16 @@ NVPRO_PYRAMID_API uint32_t nvproPyramidFastDispatch(
 
 /* nvproPyramidDefaultGeneralDispatcher (nvpro_pyramid_dispatch.hpp:247-292). */
 NVPRO_PYRAMID_API uint32_t nvproPyramidDefaultGeneralDispatcher(
+    NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
+    NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state);
+
+/* A general dispatcher that blits one level instead of dispatching the
+ * general pipeline (it binds pipelineIfNeeded when given, for the preset):
+ * nvproCmdPyramidDispatchEx with it and nvproPyramidDefaultFastDispatcher is
+ * the demo's "generalblit" mode -- the fast pipeline where the sizes allow
+ * it, a linear blit of one level otherwise (demo_app/mipmap_pipelines.cpp:
+ * 350-452, pipeline_alternative.cpp:16).  Returns 1. */
+NVPRO_PYRAMID_API uint32_t nvproPyramidBlitGeneralDispatcher(
     NvproPyramidCmd cmdBuf, const void* layout, uint32_t pushConstantOffset,
     NvproPyramidPipeline pipelineIfNeeded, const NvproPyramidState* state);
 

@@ -431,6 +431,48 @@ void generalDispatch(const Image& img, uint32_t L, uint32_t n, uint64_t groups, 
   }
 }
 
+// Linear blit of level L to L + 1 (vkCmdBlitImage, VK_FILTER_LINEAR; the
+// fallback of demo_app/mipmap_pipelines.cpp:408-423), with the library's
+// pinned FP32 filter: per axis scale = src / dst, u = (x + 0.5) * scale - 0.5,
+// i = floor(u), a = u - i, taps i and i + 1 clamped to the edge; rows lerped
+// first (t0 * (1 - a) + t1 * a), then the column; STORE encoding.
+void blitLevel(const Image& img, uint32_t L) {
+  const uint32_t sw = img.w[L], sh = img.h[L], dw = img.w[L + 1], dh = img.h[L + 1];
+  struct Tap {
+    uint32_t i0, i1;
+    float a;
+  };
+  auto axis = [](uint32_t x, uint32_t src, uint32_t dst) {
+    const float scale = (float)src / (float)dst;
+    const float t = (float)x + 0.5f;
+    const float u = t * scale - 0.5f;
+    const float f = std::floor(u);
+    Tap r;
+    r.a = u - f;
+    const int i = (int)f;
+    r.i0 = (uint32_t)std::min(std::max(i, 0), (int)src - 1);
+    r.i1 = (uint32_t)std::min(std::max(i + 1, 0), (int)src - 1);
+    return r;
+  };
+  auto lerp = [](const Vec4& t0, const Vec4& t1, float a) {
+    const float b = 1.0f - a;
+    Vec4 r;
+    for (int c = 0; c < 4; ++c) {
+      const float p0 = t0.v[c] * b;
+      const float p1 = t1.v[c] * a;
+      r.v[c] = p0 + p1;
+    }
+    return r;
+  };
+  for (uint32_t y = 0; y < dh; ++y)
+    for (uint32_t x = 0; x < dw; ++x) {
+      const Tap ax = axis(x, sw, dw), ay = axis(y, sh, dh);
+      const Vec4 r0 = lerp(img.load(L, ax.i0, ay.i0), img.load(L, ax.i1, ay.i0), ax.a);
+      const Vec4 r1 = lerp(img.load(L, ax.i0, ay.i1), img.load(L, ax.i1, ay.i1), ax.a);
+      img.store(L + 1, x, y, lerp(r0, r1, ay.a));
+    }
+}
+
 uint32_t fullLevels(uint32_t w, uint32_t h) {
   uint32_t m = 0;
   while (w != 0 || h != 0) {
@@ -657,7 +699,8 @@ int orc_default_schedule(uint32_t w, uint32_t h, uint32_t mipLevels, int hasFast
 }
 
 // Run a dispatch sequence (shader semantics) on a packed image whose level 0
-// is filled.  preset: 1 sRGBA8, 2 RGBA32F, 3 RGBA16F.  fastShared /
+// is filled.  preset: 1 sRGBA8, 2 RGBA32F, 3 RGBA16F.  isFast: 1 fast
+// dispatch, 0 general dispatch, 2 linear blit of one level.  fastShared /
 // generalShared: shared-memory format of the fast / general pipeline
 // (0 FP32, 1 SRGB_SHARED, 2 F16_SHARED; sRGBA8 only).
 int orc_run_ex(int preset, int fastShared, int generalShared, uint32_t w, uint32_t h, uint32_t mipLevels,
@@ -670,7 +713,10 @@ int orc_run_ex(int preset, int fastShared, int generalShared, uint32_t w, uint32
   for (int i = 0; i < count; ++i) {
     const uint32_t L = pc[i] >> 5, n = pc[i] & 31u;
     if (n == 0 || L + n >= mipLevels) return -2;
-    if (isFast[i]) {
+    if (isFast[i] == 2) {  // a linear blit of one level
+      if (n != 1) return -3;
+      blitLevel(img, L);
+    } else if (isFast[i]) {
       if (n > 6 || (img.w[L] % (1u << n)) || (img.h[L] % (1u << n))) return -3;
       fastDispatch(img, L, n, groups[i], fastShared);
     } else {

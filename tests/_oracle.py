@@ -77,6 +77,27 @@ def default_schedule(w, h, mips=0, has_fast=True, div=4, max_levels=6):
 SHARED_FP32, SHARED_SRGB, SHARED_F16 = 0, 1, 2
 
 
+def fast_or_blit_schedule(w, h, mips=0):
+    """The demo's "generalblit" sequence (demo_app/mipmap_pipelines.cpp:
+    350-452): the default fast dispatcher <4, 6> where it accepts the level,
+    else a linear blit of one level (isFast = 2)."""
+    mips = mips or full_levels(w, h)
+    out, level, remaining, x, y = [], 0, mips - 1, w, h
+    while remaining:
+        if x % 4 == 0 and y % 4 == 0:
+            tx, ty, done = x, y, 0
+            while tx % 2 == 0 and ty % 2 == 0 and done < remaining and done < 6:
+                tx, ty, done = tx // 2, ty // 2, done + 1
+            shift, mask = (12, 4095) if done > 5 else (10, 1023)
+            out.append((1, level << 5 | done, ((x * y + mask) & 0xFFFFFFFF) >> shift))
+        else:
+            done = 1
+            out.append((2, level << 5 | 1, 1))
+        level, remaining = level + done, remaining - done
+        x, y = max(x >> done, 1), max(y >> done, 1)
+    return out
+
+
 def run(preset: int, w: int, h: int, packed: np.ndarray, schedule=None, mips: int = 0, fast_shared: int = 0,
         general_shared: int = 0) -> np.ndarray:
     """Apply a dispatch schedule (default: the reference's) to a packed image in

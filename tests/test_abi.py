@@ -204,3 +204,18 @@ def test_premultiply_argument_checks(native):
     assert f(None, base, 16, base, 0, 8, 8) == N.ERROR_INVALID_ARGUMENT  # pitch below 4 * width
     assert f(None, base + 2, 0, base + 2, 0, 8, 8) == N.ERROR_UNSUPPORTED  # texels not 4-byte aligned
     assert f(None, base, 0, base + 64, 0, 8, 8) == N.ERROR_INVALID_ARGUMENT  # overlapping, not equal
+
+
+def test_general_blit_mode_records(native):
+    """nvproCmdPyramidDispatchEx with nvproPyramidBlitGeneralDispatcher: the
+    demo's generalblit loop -- the fast dispatcher where it accepts a level,
+    else one blit record per level."""
+    blit = P.blit_general_dispatcher()
+    for w, h in [(1920, 1080), (4095, 4095), (2052, 2052), (2048, 2048), (5, 3), (1, 9), (64, 1)]:
+        recs = record(w, h, general=blit)
+        got = [(2 if r["isBlit"] else r["isFastPipeline"], r["pushConstant"],
+                r["groupCountX"] if r["isFastPipeline"] else 1) for r in recs]
+        assert got == O.fast_or_blit_schedule(w, h), (w, h)
+    cmd = P.Cmd(N.CMD_RECORD_ONLY)
+    cmd.begin(None)
+    expect_error(N.ERROR_INVALID_STATE, lambda: N.check(native.nvproPyramidCmdBlitLevel(cmd.handle, 0)))

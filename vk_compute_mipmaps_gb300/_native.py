@@ -77,6 +77,7 @@ class NvproPyramidDispatchRecord(ctypes.Structure):
         ("pipelineBound", c_uint32),
         ("barrierBefore", c_uint32),
         ("configBits", c_uint32),
+        ("isBlit", c_uint32),
     ]
 
 
@@ -136,6 +137,9 @@ SIGNATURES = {
                                                      POINTER(NvproPyramidState)]),
     "nvproPyramidFastDispatch": (c_uint32, [c_void_p, c_void_p, c_uint32, c_void_p, POINTER(NvproPyramidState),
                                             c_uint32, c_uint32]),
+    "nvproPyramidCmdBlitLevel": (c_int, [c_void_p, c_uint32]),
+    "nvproPyramidBlitGeneralDispatcher": (c_uint32, [c_void_p, c_void_p, c_uint32, c_void_p,
+                                                     POINTER(NvproPyramidState)]),
     "nvproPyramidDefaultGeneralDispatcher": (c_uint32, [c_void_p, c_void_p, c_uint32, c_void_p,
                                                         POINTER(NvproPyramidState)]),
     "nvproPyramidCmdDeviceStatus": (c_int, [c_void_p]),

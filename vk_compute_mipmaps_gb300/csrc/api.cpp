@@ -110,6 +110,7 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
   const uint32_t n = rec.info.pushConstant & 31u;
   const uint32_t bpp = presetBytes(rec.info.preset);
   if (n == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "dispatch with level count 0");
+  if (rec.info.isBlit && n != 1) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "a blit fills one level");
   if (rec.info.isFastPipeline ? n > kMaxDispatchLevels : n > 2)
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%s pipeline cannot fill %u levels in one dispatch",
                 rec.info.isFastPipeline ? "fast" : "general", n);
@@ -120,6 +121,7 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
   out->batch = 1;  // one image unless a strided call says otherwise
   out->preset = rec.info.preset;
   out->isFast = rec.info.isFastPipeline;
+  out->isBlit = rec.info.isBlit;
   out->inputLevel = L;
   out->levelCount = n;
   out->groups = (rec.info.groupCountY == 0 || rec.info.groupCountZ == 0) ? 0 : rec.info.groupCountX;
@@ -366,6 +368,31 @@ NvproPyramidResult nvproPyramidCmdDispatch(NvproPyramidCmd cmd, uint32_t gx, uin
   return NVPRO_PYRAMID_SUCCESS;
 }
 
+NvproPyramidResult nvproPyramidCmdBlitLevel(NvproPyramidCmd cmd, uint32_t srcLevel) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->recording) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
+  if (!cmd->pipeline) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "blit with no bound pipeline (preset)");
+  if (!cmd->imageBound) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "blit with no bound image");
+  if (srcLevel >= 31) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "source level %u", srcLevel);
+  Record r;
+  std::memset(&r, 0, sizeof r);
+  r.info.isFastPipeline = 0;
+  r.info.isBlit = 1;
+  r.info.preset = cmd->pipeline->preset;
+  r.info.pushConstant = srcLevel << NVPRO_PYRAMID_INPUT_LEVEL_SHIFT | 1u;
+  r.info.groupCountX = r.info.groupCountY = r.info.groupCountZ = 1;
+  r.info.pipelineBound = cmd->pipelineBoundSinceDispatch;
+  r.info.barrierBefore = cmd->barrierSinceDispatch;
+  r.image = cmd->image;
+  DispatchParams probe;
+  NvproPyramidResult res = makeParams(r, &probe);
+  if (res != NVPRO_PYRAMID_SUCCESS) return cmdFail(cmd, res, "%s", t_lastError.c_str());
+  cmd->records.push_back(r);
+  cmd->pipelineBoundSinceDispatch = false;
+  cmd->barrierSinceDispatch = false;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
 NvproPyramidResult nvproPyramidCmdPipelineBarrier(NvproPyramidCmd cmd) {
   if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
   if (!cmd->recording) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "command is not recording");
@@ -500,6 +527,17 @@ uint32_t nvproPyramidDefaultGeneralDispatcher(NvproPyramidCmd cmdBuf, const void
   else
     nvproPyramidCmdDispatch(cmdBuf, ((dstW + kTile - 1) / kTile) * ((dstH + kTile - 1) / kTile), 1u, 1u);
   return levels;
+}
+
+uint32_t nvproPyramidBlitGeneralDispatcher(NvproPyramidCmd cmdBuf, const void* /*layout*/,
+                                           uint32_t /*pushConstantOffset*/, NvproPyramidPipeline pipelineIfNeeded,
+                                           const NvproPyramidState* state) {
+  if (!state) {
+    cmdFail(cmdBuf, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "state is NULL");
+    return 0;
+  }
+  if (pipelineIfNeeded) nvproPyramidCmdBindPipeline(cmdBuf, pipelineIfNeeded);
+  return nvproPyramidCmdBlitLevel(cmdBuf, state->currentLevel) == NVPRO_PYRAMID_SUCCESS ? 1u : 0u;
 }
 
 NvproPyramidResult nvproCmdPyramidDispatchEx(NvproPyramidCmd cmdBuf, NvproPyramidPipelines pipelines,

@@ -44,6 +44,7 @@ struct DispatchParams {
   // Format of the values handed through the reference's shared memory
   // (sRGBA8 only): kSharedFp32, kSharedSrgb or kSharedF16.
   uint32_t sharedFmt;
+  uint32_t isBlit;  // a linear blit of one level (isFast 0, levelCount 1)
   LevelView lv[kMaxDispatchLevels + 1];
   // Strided batches (portable kernels only): `batch` images, image i's level
   // L+k at lv[k].ptr + i * imageStride[k].

@@ -124,7 +124,7 @@ void makeStage(const DispatchParams& p, uint64_t warpsResident, Stage* g) {
 }  // namespace
 
 bool generalFastSupported(const DispatchParams& p) {
-  if (p.preset != kSrgba8 || p.isFast || (p.levelCount != 1 && p.levelCount != 2)) return false;
+  if (p.preset != kSrgba8 || p.isFast || p.isBlit || (p.levelCount != 1 && p.levelCount != 2)) return false;
   const LevelView &l0 = p.lv[0], &l1 = p.lv[1];
   if (l0.w < 2 || l0.h < 2) return false;  // one-tap axes stay on the portable kernels
   if (p.levelCount == 1) return p.groups * 128u >= uint64_t(l1.w) * l1.h;

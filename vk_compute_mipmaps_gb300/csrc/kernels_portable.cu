@@ -248,9 +248,61 @@ __global__ void __launch_bounds__(kThreads) portableGeneral2Kernel(DispatchParam
   }
 }
 
+// ---------------------------------------------------------------------------
+// Linear blit of one level (vkCmdBlitImage with VK_FILTER_LINEAR, the
+// fallback of the demo's "generalblit" mode, demo_app/mipmap_pipelines.cpp:
+// 408-423): destination texel (x, y) samples the source at
+// ((x + 0.5) srcW / dstW, (y + 0.5) srcH / dstH), bilinear on decoded values
+// with clamp-to-edge, each FP32 operation rounded as the header states.
+struct BlitAxis {
+  uint32_t i0, i1;  // source texels (clamped)
+  float a;          // weight of i1
+};
+
+__device__ __forceinline__ BlitAxis blitAxis(uint32_t x, uint32_t srcSize, uint32_t dstSize) {
+  const float scale = __fdiv_rn(__uint2float_rn(srcSize), __uint2float_rn(dstSize));
+  const float u = __fsub_rn(__fmul_rn(__fadd_rn(__uint2float_rn(x), 0.5f), scale), 0.5f);
+  const float f = floorf(u);
+  BlitAxis r;
+  r.a = __fsub_rn(u, f);
+  const int i = int(f);
+  r.i0 = uint32_t(min(max(i, 0), int(srcSize) - 1));
+  r.i1 = uint32_t(min(max(i + 1, 0), int(srcSize) - 1));
+  return r;
+}
+
+__device__ __forceinline__ float4 lerp4(float4 t0, float4 t1, float a) {
+  const float b = __fsub_rn(1.0f, a);
+  return f4add(f4scale(b, t0), f4scale(a, t1));
+}
+
+template <uint32_t P>
+__global__ void __launch_bounds__(kThreads) portableBlitKernel(DispatchParams p) {
+  __shared__ SrgbTablesSmem tabs;
+  if (P == kSrgba8) {
+    loadSrgbTables(&tabs);
+    __syncthreads();
+  }
+  const TexelIO<P> io = makeIO<P>(&tabs);
+  constexpr uint32_t B = TexelIO<P>::kBytes;
+  const LevelView src = levelOf(p, 0), dst = levelOf(p, 1);
+  const uint64_t total = uint64_t(dst.w) * dst.h;
+  for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < total; i += uint64_t(gridDim.x) * kThreads) {
+    const uint32_t x = uint32_t(i % dst.w), y = uint32_t(i / dst.w);
+    const BlitAxis ax = blitAxis(x, src.w, dst.w), ay = blitAxis(y, src.h, dst.h);
+    const float4 r0 = lerp4(io.load(texelAddr(src, ax.i0, ay.i0, B)), io.load(texelAddr(src, ax.i1, ay.i0, B)), ax.a);
+    const float4 r1 = lerp4(io.load(texelAddr(src, ax.i0, ay.i1, B)), io.load(texelAddr(src, ax.i1, ay.i1, B)), ax.a);
+    io.store(texelAddr(dst, x, y, B), lerp4(r0, r1, ay.a));
+  }
+}
+
 template <uint32_t P>
 cudaError_t launchPreset(const DispatchParams& p, cudaStream_t stream, uint32_t* launches) {
-  if (p.isFast) {
+  if (p.isBlit) {
+    const uint64_t total = uint64_t(p.lv[1].w) * p.lv[1].h;
+    const uint64_t blocks = std::min<uint64_t>((total + kThreads - 1) / kThreads, 152u * 64u);
+    portableBlitKernel<P><<<dim3(uint32_t(blocks), 1, p.batch), kThreads, 0, stream>>>(p);
+  } else if (p.isFast) {
     const uint32_t n = p.levelCount;
     const uint32_t coverW = (p.lv[0].w >> n) << n, coverH = (p.lv[0].h >> n) << n;
     const uint64_t regions = uint64_t((coverW + kRegion - 1) / kRegion) * ((coverH + kRegion - 1) / kRegion);

@@ -192,6 +192,14 @@ def cmd_pyramid_dispatch(cmd: Cmd, pipelines: Pipelines, width: int, height: int
             "nvproCmdPyramidDispatchEx")
 
 
+def blit_general_dispatcher():
+    """The library's nvproPyramidBlitGeneralDispatcher as a dispatcher
+    callback: with it as the general dispatcher, cmd_pyramid_dispatch is the
+    demo's "generalblit" mode (fast pipeline where possible, else a linear
+    blit of one level)."""
+    return N.DISPATCHER(("nvproPyramidBlitGeneralDispatcher", N.load()))
+
+
 # ---------------------------------------------------------------------------
 # torch convenience: packed mip chains on the GPU.
 
