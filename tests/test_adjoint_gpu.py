@@ -193,3 +193,45 @@ def test_autograd_with_base_takes_level0_gradient(cuda):
     assert torch.equal(base.grad, adjoint(ups, tuple(base.shape), torch.float32, cuda))
     ref = dense_adjoint([u[0].double().cpu().numpy() for u in ups], W, H)
     assert rel_err(base.grad[0].double().cpu().numpy(), ref) <= RTOL
+
+
+@pytest.mark.parametrize("shape", [(8, 256, 256), (1, 777, 1023), (2, 64, 48)])
+def test_autograd_step_captures_in_cuda_graph(cuda, shape):
+    """Forward + backward through the autograd Function captured in a CUDA
+    graph (no host synchronisation, allocations from torch's allocator):
+    replays give the eager gradient, also after the input changes in place."""
+    import torch
+
+    from vk_compute_mipmaps_gb300 import autograd as A
+    B, H, W = shape
+    g = torch.Generator(device=cuda).manual_seed(B * H + W)
+    base = torch.rand((B, H, W, 4), generator=g, device=cuda).requires_grad_(True)
+    ups = [torch.randn((B, h, w, 4), generator=g, device=cuda) for w, h in P.level_sizes(W, H)[1:]]
+
+    def step():
+        base.grad = None
+        torch.autograd.backward(A.pyramid(base), ups)
+
+    side = torch.cuda.Stream(cuda)
+    side.wait_stream(torch.cuda.current_stream(cuda))
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            step()
+    torch.cuda.current_stream(cuda).wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    base.grad = None
+    with torch.cuda.graph(graph):
+        levels = A.pyramid(base)
+        torch.autograd.backward(levels, ups)
+    static_grad = base.grad
+    for _ in range(2):
+        with torch.no_grad():
+            base.mul_(0.5).add_(0.25)
+            for u in ups:
+                u.mul_(-1.0)
+        graph.replay()
+        torch.cuda.synchronize()
+        want = A.adjoint([None] + ups, (B, H, W, 4), torch.float32, cuda)
+        assert torch.equal(static_grad, want)
+        eager = A.forward_levels(base.detach())
+        assert all(torch.equal(a, b) for a, b in zip(levels, eager))
