@@ -71,7 +71,7 @@ __device__ __forceinline__ uint32_t premultiplyTexel(uint32_t t, uint32_t tab) {
   return __byte_perm(__byte_perm(r, g, 0x0040), __byte_perm(b, t, 0x0070), 0x5410);
 }
 
-__global__ void __launch_bounds__(kThreads) premultiplyKernel(const PremulParams p) {
+__global__ void __launch_bounds__(kThreads, 3) premultiplyKernel(const PremulParams p) {
   extern __shared__ __align__(128) uint8_t smem[];
   for (uint32_t i = threadIdx.x; i < kSmemBytes / 16; i += kThreads)
     reinterpret_cast<uint4*>(smem)[i] = reinterpret_cast<const uint4*>(g_premulTable)[i];
