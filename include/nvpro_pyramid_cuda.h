@@ -267,6 +267,15 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidPremultiplyAlpha(
     NvproPyramidStream stream, const void* src, uint64_t srcPitch, void* dst, uint64_t dstPitch,
     uint32_t width, uint32_t height);
 
+/* Test support for failure detection (no reference counterpart): launch, on
+ * the command's stream, one small kernel whose bounded device-side wait runs
+ * out -- waitKind 0: the fast kernel's mbarrier wait on a phase nothing
+ * completes; 1: the general chain's grid barrier that nothing releases.  It
+ * gives up after its limit (about a second) and sets the command's error
+ * flag, so the next nvproPyramidCmdDeviceStatus reports
+ * NVPRO_PYRAMID_ERROR_TIMEOUT and resets the counters; nothing faults. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugForceWaitTimeout(NvproPyramidCmd cmd, uint32_t waitKind);
+
 /* Test support (no reference counterpart): encode n floats of x (device
  * memory) with the kernels' fast sRGB encoder into `fast` (inputs clamped to
  * its domain [0, 1] first), and with the exact threshold count into `exact`. */

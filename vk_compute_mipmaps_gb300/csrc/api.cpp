@@ -619,6 +619,20 @@ NvproPyramidResult nvproPyramidCmdDeviceStatus(NvproPyramidCmd cmd) {
   return NVPRO_PYRAMID_SUCCESS;
 }
 
+NvproPyramidResult nvproPyramidDebugForceWaitTimeout(NvproPyramidCmd cmd, uint32_t waitKind) {
+  if (!validCmd(cmd)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid command object");
+  if (!cmd->scratch.counters) return fail(NVPRO_PYRAMID_ERROR_INVALID_STATE, "command without device counters");
+  cudaError_t e;
+  if (waitKind == 0)
+    e = launchDebugMbarTimeout(cmd->scratch.counters + kCounterError, cmd->stream);
+  else if (waitKind == 1)
+    e = launchDebugGridBarrierTimeout(cmd->scratch, cmd->stream);
+  else
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "waitKind %u", waitKind);
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "launch failed: %s", cudaGetErrorString(e));
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
 NvproPyramidResult nvproPyramidSpeedOfLightProbe(NvproPyramidStream stream, const NvproPyramidImage* pImage,
                                                 uint32_t mipLevels) {
   if (!pImage) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pImage is NULL");

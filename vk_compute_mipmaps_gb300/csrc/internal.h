@@ -125,6 +125,12 @@ cudaError_t launchPremultiply(const uint8_t* src, uint64_t srcPitch, uint8_t* ds
 cudaError_t launchProbe(const uint8_t* const* levels, const uint64_t* pitches, uint32_t width, uint32_t height,
                         uint32_t levelCount, cudaStream_t stream);
 
+// Test support for failure detection: a bounded wait that runs out (an
+// mbarrier phase nothing completes; a grid barrier nothing releases) and
+// sets the error flag of `scratch` / errorFlag.
+cudaError_t launchDebugMbarTimeout(uint32_t* errorFlag, cudaStream_t stream);
+cudaError_t launchDebugGridBarrierTimeout(const Scratch& scratch, cudaStream_t stream);
+
 cudaError_t launchAdjointChain(const AdjointChainParams& p, cudaStream_t stream);
 cudaError_t launchAdjointLevel(const AdjointLevelParams& p, cudaStream_t stream);
 

@@ -71,6 +71,20 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
   }
 }
 
+// Test support for failure detection: one CTA arrives at the chain kernels'
+// bounded grid barrier with the arrival count raised by two, as if two CTAs
+// had arrived that will never release it; the wait gives up after its limit
+// and sets the error flag.  The counters are left for the host to reset.
+__global__ void debugGridBarrierTimeoutKernel(uint32_t* count, uint32_t* genWord, uint32_t* errorFlag) {
+  __shared__ uint32_t okFlag;
+  uint32_t gen = 0;
+  if (threadIdx.x == 0) {
+    atomicAdd(count, 2u);
+    gen = ldAcquire(genWord);
+  }
+  gridBarrierWait(count, genWord, errorFlag, gen, &okFlag);
+}
+
 struct DeviceState {
   int sms = 0;
   int ctasPerSm = 0;
@@ -134,6 +148,14 @@ bool generalFastSupported(const DispatchParams& p) {
 }
 
 uint32_t generalMaxStages() { return kMaxStages; }
+
+cudaError_t launchDebugGridBarrierTimeout(const Scratch& scratch, cudaStream_t stream) {
+  if (scratch.counterCount <= kCounterBarrierGen) return cudaErrorInvalidValue;
+  debugGridBarrierTimeoutKernel<<<1, 32, 0, stream>>>(scratch.counters + kCounterBarrier,
+                                                       scratch.counters + kCounterBarrierGen,
+                                                       scratch.counters + kCounterError);
+  return cudaGetLastError();
+}
 
 cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStream_t stream, const Scratch& scratch,
                                uint32_t* launches) {

@@ -535,6 +535,21 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+// Test support for failure detection: one warp waits, with the kernels' own
+// bounded mbarrier wait, on a phase that nothing completes (no thread
+// arrives); the wait gives up after its time limit and the error flag is set,
+// as a stalled TMA load would leave it.  Nothing is in flight when it exits.
+__global__ void debugMbarTimeoutKernel(uint32_t* errorFlag) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t addr = smemAddr(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(addr) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (threadIdx.x == 0 && !mbarWait(addr, 0)) atomicExch(errorFlag, 1u);
+}
+
 // Encode every float of x (test support for the exhaustive codec check).
 // alpha = 0: the value goes through the packed texel encoder as colour
 // channel i % 3, with its neighbours in the array as the other channels, and
@@ -735,6 +750,11 @@ cudaError_t staticScratch(uint32_t** ptr) {
   }
   *ptr = addrs[dev];
   return cudaSuccess;
+}
+
+cudaError_t launchDebugMbarTimeout(uint32_t* errorFlag, cudaStream_t stream) {
+  debugMbarTimeoutKernel<<<1, 32, 0, stream>>>(errorFlag);
+  return cudaGetLastError();
 }
 
 cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, uint32_t alpha,
