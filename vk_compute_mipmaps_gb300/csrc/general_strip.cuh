@@ -120,13 +120,20 @@ __device__ __forceinline__ float4 decodeAligned(uint32_t w, const Lut& L) {
 // kernel free of calls.  SF: the pipeline's shared format, applied to the
 // level-(L+1) values that level L+2 is reduced from (sharedLevel_,
 // nvpro_pyramid.glsl:664,717).
-template <uint32_t SF>
+// strip<SF, V>: V fixes the stage's variant at compile time, or kRuntimeVariant
+// reads it once from the stage (measured: a single read of the variant instead
+// of one per flag took 4095^2 from 75.8 to 73.7 us and the 256-image batch
+// from 1454 to 1375 us; a second, variant-15 copy in the chain kernel spilled).
+constexpr uint32_t kRuntimeVariant = 255;
+
+template <uint32_t SF, uint32_t V = kRuntimeVariant>
 __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t band, uint32_t lane, const Lut& lut) {
-  const uint32_t LEVELS = st.variant >= 16 ? 1u : 2u;
-  const bool TX0 = LEVELS == 2 ? (st.variant & 8) != 0 : (st.variant & 2) != 0;
-  const bool TY0 = LEVELS == 2 ? (st.variant & 4) != 0 : (st.variant & 1) != 0;
-  const bool TX1 = LEVELS == 2 && (st.variant & 2) != 0;
-  const bool TY1 = LEVELS == 2 && (st.variant & 1) != 0;
+  const uint32_t variant = V == kRuntimeVariant ? st.variant : V;
+  const uint32_t LEVELS = variant >= 16 ? 1u : 2u;
+  const bool TX0 = LEVELS == 2 ? (variant & 8) != 0 : (variant & 2) != 0;
+  const bool TY0 = LEVELS == 2 ? (variant & 4) != 0 : (variant & 1) != 0;
+  const bool TX1 = LEVELS == 2 && (variant & 2) != 0;
+  const bool TY1 = LEVELS == 2 && (variant & 1) != 0;
   // Every field in a register before the first store: stores through
   // generic pointers would otherwise force reloads of a stage held in memory.
   const Lut L = lut;
