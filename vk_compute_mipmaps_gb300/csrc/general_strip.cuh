@@ -126,7 +126,11 @@ __device__ __forceinline__ float4 decodeAligned(uint32_t w, const Lut& L) {
 // from 1454 to 1375 us; a second, variant-15 copy in the chain kernel spilled).
 constexpr uint32_t kRuntimeVariant = 255;
 
-template <uint32_t SF, uint32_t V = kRuntimeVariant>
+// ROWS: level-(L+1) rows whose level-L rows load together (the prefetch
+// depth); 4 in the chain kernel, 2 in the batch kernel, whose units are
+// shorter (measured: 2 rows took the 256-image batch from 1375 to 1313 us
+// but the 4095^2 chain from 74 to 78 us).
+template <uint32_t SF, uint32_t V = kRuntimeVariant, uint32_t ROWS = kGroupRows>
 __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t band, uint32_t lane, const Lut& lut) {
   const uint32_t variant = V == kRuntimeVariant ? st.variant : V;
   const uint32_t LEVELS = variant >= 16 ? 1u : 2u;
@@ -185,10 +189,10 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
   // <= h0 - 1 with two).
   const uint32_t dB = uint32_t(colB - colA);  // 4, or 0 where column 2x+1 is clamped
   const uint64_t pitch = p.srcPitch;
-  auto ldGroup = [&](uint32_t yg, uint32_t (&raw)[kGroupRows][4]) {
+  auto ldGroup = [&](uint32_t yg, uint32_t (&raw)[ROWS][4]) {
     const uint8_t* row = colA + uint64_t(TY0 ? 2 * yg + 1 : 2 * yg) * pitch;
 #pragma unroll
-    for (uint32_t j = 0; j < kGroupRows; ++j) {
+    for (uint32_t j = 0; j < ROWS; ++j) {
       if (yg + j < ye) {
         raw[j][0] = ldTexel(row);
         raw[j][1] = ldTexel(row + dB);
@@ -207,9 +211,9 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
   }
   float4 h0v = make_float4(0.f, 0.f, 0.f, 0.f), h1v = h0v;  // level-(L+1) rows 2Y, 2Y+1
 
-  auto process = [&](uint32_t yg, const uint32_t (&raw)[kGroupRows][4]) {
+  auto process = [&](uint32_t yg, const uint32_t (&raw)[ROWS][4]) {
 #pragma unroll
-    for (uint32_t j = 0; j < kGroupRows; ++j) {
+    for (uint32_t j = 0; j < ROWS; ++j) {
       const uint32_t y = yg + j;
       if (y >= ye) break;
       const float4 r1a = decodeAligned(raw[j][0], L), r1b = decodeAligned(raw[j][1], L);
@@ -269,16 +273,16 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
   };
 
   // two row buffers in turn: the next group's rows load while this one reduces
-  uint32_t bufA[kGroupRows][4], bufB[kGroupRows][4];
+  uint32_t bufA[ROWS][4], bufB[ROWS][4];
   ldGroup(yb, bufA);
   for (uint32_t yg = yb;;) {
-    if (yg + kGroupRows < ye) ldGroup(yg + kGroupRows, bufB);
+    if (yg + ROWS < ye) ldGroup(yg + ROWS, bufB);
     process(yg, bufA);
-    yg += kGroupRows;
+    yg += ROWS;
     if (yg >= ye) break;
-    if (yg + kGroupRows < ye) ldGroup(yg + kGroupRows, bufA);
+    if (yg + ROWS < ye) ldGroup(yg + ROWS, bufA);
     process(yg, bufB);
-    yg += kGroupRows;
+    yg += ROWS;
     if (yg >= ye) break;
   }
 }
