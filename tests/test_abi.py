@@ -204,6 +204,7 @@ def test_premultiply_argument_checks(native):
     assert f(None, base, 16, base, 0, 8, 8) == N.ERROR_INVALID_ARGUMENT  # pitch below 4 * width
     assert f(None, base + 2, 0, base + 2, 0, 8, 8) == N.ERROR_UNSUPPORTED  # texels not 4-byte aligned
     assert f(None, base, 0, base + 64, 0, 8, 8) == N.ERROR_INVALID_ARGUMENT  # overlapping, not equal
+    assert f(None, base, 32, base, 64, 8, 8) == N.ERROR_INVALID_ARGUMENT  # same start, different pitches
 
 
 def test_general_blit_mode_records(native):

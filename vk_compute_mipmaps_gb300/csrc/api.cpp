@@ -665,10 +665,12 @@ NvproPyramidResult nvproPyramidPremultiplyAlpha(NvproPyramidStream stream, const
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "row pitch below 4 * width");
   if ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst) | srcPitch | dstPitch) % 4)
     return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "texels must be 4-byte aligned");
-  if (src != dst && srcPitch == dstPitch) {  // overlapping but distinct images are not supported
+  // in place (same pointer and pitch) or disjoint byte ranges; a partial overlap would race
+  if (src != dst || srcPitch != dstPitch) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(src), b = reinterpret_cast<uintptr_t>(dst);
-    const uint64_t bytes = srcPitch * (height - 1) + uint64_t(width) * 4;
-    if (a < b + bytes && b < a + bytes)
+    const uint64_t aBytes = srcPitch * (height - 1) + uint64_t(width) * 4;
+    const uint64_t bBytes = dstPitch * (height - 1) + uint64_t(width) * 4;
+    if (a < b + bBytes && b < a + aBytes)
       return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "source and destination overlap without being equal");
   }
   const cudaError_t e = launchPremultiply(static_cast<const uint8_t*>(src), srcPitch, static_cast<uint8_t*>(dst),
