@@ -358,8 +358,8 @@ def premultiply_alpha(src, dst=None, stream: Optional[int] = None):
     return dst
 
 
-def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Optional[int] = None, bands: int = 8,
-                       flags: int = 0, premultiply: bool = False) -> None:
+def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Optional[int] = None,
+                       bands: Optional[int] = None, flags: int = 0, premultiply: bool = False) -> None:
     """Level 0 from pinned host memory (`host_base`, chain.offsets[1] bytes),
     levels 1.. back to pinned host memory (`host_levels`, the rest of the
     packed chain), with the copies overlapped with the generation.
@@ -370,7 +370,9 @@ def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Option
     previous band's levels 1..n are copied out; the remaining dispatches run
     on level n after the last band.  The dispatches, and so the bytes, are
     those of `generate` on the whole chain.  Otherwise: copy in, generate,
-    copy out.  With `premultiply` (sRGBA8), each band of level 0 is
+    copy out.  `bands` defaults to one per 32 MiB of level 0, at most 32
+    (16384^2: 32 bands, 5.58 ms against 5.72 with 8 and 5.93 with 4; the host
+    link's 210 GB/s make the upload alone 5.1 ms).  With `premultiply` (sRGBA8), each band of level 0 is
     premultiplied in place on the device right after its copy, as the
     reference's -do-premultiply-alpha staging does before the pyramid (the
     host copy of level 0 is left as it was).  Returns when the work is
@@ -379,6 +381,8 @@ def generate_from_host(chain: "MipChain", host_base, host_levels, stream: Option
     dev = chain.storage.device
     cur = torch.cuda.current_stream(dev) if stream is None else torch.cuda.ExternalStream(stream, device=dev)
     off = chain.offsets
+    if bands is None:
+        bands = max(1, min(32, off[1] >> 25))
     n = _first_fast_levels(chain.width, chain.height, chain.levels)
     rows_unit = 1 << n
     band_rows = -(-chain.height // max(bands, 1) // rows_unit) * rows_unit if n else chain.height
