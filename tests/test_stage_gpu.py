@@ -57,8 +57,9 @@ def test_premultiply_layouts(cuda, w, h, layout):
     assert np.array_equal(got.cpu().numpy(), want), layout
 
 
-@pytest.mark.parametrize("w,h", [(2048, 2048), (1920, 1080), (4096, 64)])
-def test_generate_from_host_premultiply(cuda, w, h):
+@pytest.mark.parametrize("w,h,bands", [(2048, 2048, 8), (2048, 2048, None), (1920, 1080, 4), (4096, 64, None),
+                                       (8192, 8192, None)])
+def test_generate_from_host_premultiply(cuda, w, h, bands):
     import torch
     base = np.random.default_rng(w + h).integers(0, 256, (h, w, 4), dtype=np.uint8)
     ref = V.MipChain(w, h, V.PRESET_SRGBA8, device=cuda)
@@ -67,7 +68,7 @@ def test_generate_from_host_premultiply(cuda, w, h):
     chain = V.MipChain(w, h, V.PRESET_SRGBA8, device=cuda)
     host_base = torch.from_numpy(base.reshape(-1).copy()).pin_memory()
     host_levels = torch.empty(chain.offsets[-1] - chain.offsets[1], dtype=torch.uint8).pin_memory()
-    V.generate_from_host(chain, host_base, host_levels, premultiply=True)
+    V.generate_from_host(chain, host_base, host_levels, bands=bands, premultiply=True)
     torch.cuda.synchronize()
     assert torch.equal(chain.storage, ref.storage)  # level 0 premultiplied on the device
     assert torch.equal(host_levels, ref.storage[chain.offsets[1]:].cpu())
