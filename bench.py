@@ -35,7 +35,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 HEADLINE = (16384, 16384)
-CONFIGS = [(4096, 4096), (4095, 4095), (4094, 4094), (1920, 1080), (2048, 2048)]
+CONFIGS = [(4096, 4096), (4095, 4095), (4094, 4094), (1920, 1080), (2048, 2048),
+           # the reference's other published sizes (1440p, 4k, the all-3x3 2047^2)
+           (2560, 1440), (3840, 2160), (2047, 2047)]
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -198,6 +200,15 @@ def bench_config(w, h, dev, stream, flush, steps, content="random"):
                      "frac_of_hbm_peak": round(nbytes / (us * 1e-6) / 1e9 / peak, 4)}
     out["launches_per_chain"] = run()
     out["algorithmic_bytes"] = nbytes
+    if w >= 2 and h >= 2:  # the speed-of-light probe on the same chain (the reference's "baseline")
+        import vk_compute_mipmaps_gb300 as V
+        img = chain.image()
+        lib = V._native.load()
+        probe = lambda: V._native.check(  # noqa: E731
+            lib.nvproPyramidSpeedOfLightProbe(stream.cuda_stream, ctypes.byref(img), 0), "probe")
+        with __import__("torch").cuda.stream(stream):
+            pt = time_loop(probe, stream, steps, 3, flush=flush)
+        out["probe_l2_flushed_us"] = round(statistics.median(pt) * 1e3, 2)
     del chain
     return out
 
