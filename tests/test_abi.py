@@ -220,3 +220,30 @@ def test_general_blit_mode_records(native):
     cmd = P.Cmd(N.CMD_RECORD_ONLY)
     cmd.begin(None)
     expect_error(N.ERROR_INVALID_STATE, lambda: N.check(native.nvproPyramidCmdBlitLevel(cmd.handle, 0)))
+
+
+def test_plain_c_caller(native, repo_tmp):
+    """The header and library from a strict C99 program (gcc -pedantic
+    -Werror): the recorded schedules equal the oracle's, with config bits and
+    the blit dispatcher."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    exe = repo_tmp / "c_caller"
+    lib_dir = N.LIB_PATH.parent
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "c_caller.c"), "-o", str(exe), "-L", str(lib_dir), "-lnvpro_pyramid_cuda",
+                    f"-Wl,-rpath,{lib_dir}"], check=True)
+    for w, h, args in [(1920, 1080, []), (4095, 4095, []), (2052, 2052, ["2", "1", "0"]), (1920, 1080, ["0", "0", "1"])]:
+        out = subprocess.run([str(exe), str(w), str(h), *args], check=True, capture_output=True, text=True).stdout
+        lines = out.strip().splitlines()
+        levels = O.full_levels(w, h)
+        assert lines[0] == f"levels {levels} bytes {O.offsets(w, h, levels, 4)[-1]}"
+        recs = [tuple(map(int, ln.split())) for ln in lines[1:]]
+        fast_bits, general_bits, blit = map(int, args) if args else (0, 0, 0)
+        want = O.fast_or_blit_schedule(w, h) if blit else O.default_schedule(w, h)
+        got = [(2 if b else f, pc, g if (f or not b) else 1) for f, pc, g, b, _ in recs]
+        assert got == [tuple(x) for x in want], (w, h, args)
+        assert all(c == (fast_bits if f else general_bits) for f, _, _, b, c in recs if not b)
