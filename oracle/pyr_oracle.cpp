@@ -1,9 +1,10 @@
 // pyr_oracle.cpp -- CPU ORACLE FOR TESTS ONLY.
 //
 // This file is test infrastructure: a scalar C++ restatement of the reference
-// nvpro_pyramid mip-chain generation, used by tests/, __graft_entry__.smoke()
-// and bench.py's CPU-baseline leg as the checker.  No product code path calls
-// it.  Build: oracle/build_oracle.sh (g++ -O2 -ffp-contract=off).
+// nvpro_pyramid mip-chain generation, the oracle that tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg compare against.  No
+// product code path calls it.  Build: make -C oracle (g++ -O2
+// -ffp-contract=off).
 //
 // Parity pins (see tests/test_oracle_pins.py):
 //  * orc_refcpu_srgba8 restates the reference's own CPU generator
