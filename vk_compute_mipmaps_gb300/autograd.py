@@ -20,6 +20,7 @@ from . import _native as N
 from .pyramid import Cmd, Pipelines, level_sizes
 
 _PRESETS = {torch.float32: N.PRESET_RGBA32F, torch.float16: N.PRESET_RGBA16F}
+_ELEMENT_BYTES = {torch.float32: 4, torch.float16: 2}
 _tls = threading.local()
 
 
@@ -37,6 +38,21 @@ def _check_base(base: torch.Tensor):
         raise TypeError(f"pyramid needs float32 or float16 texels, got {base.dtype}")
     if not base.is_cuda or base.shape[-1] != 4 or base.dim() not in (3, 4):
         raise ValueError("base must be a CUDA tensor of shape [B, H, W, 4] or [H, W, 4]")
+
+
+_geometry_cache: dict = {}
+
+
+def _geometry(W: int, H: int, levels: int, esz: int):
+    """Per (W, H, levels, element size): the level sizes and the per-image
+    byte stride of every level (cached: the same for every call of a
+    training loop)."""
+    key = (W, H, levels, esz)
+    g = _geometry_cache.get(key)
+    if g is None:
+        sizes = level_sizes(W, H, levels)
+        g = _geometry_cache[key] = (sizes, _strides(sizes, esz))
+    return g
 
 
 def _strides(sizes, esz: int, present=None) -> np.ndarray:
@@ -70,14 +86,16 @@ def forward_levels(base: torch.Tensor, levels: int = 0) -> list[torch.Tensor]:
     b4 = b4.contiguous()
     B, H, W, _ = b4.shape
     preset = _PRESETS[b4.dtype]
-    sizes = level_sizes(W, H, levels)
+    sizes, strides = _geometry(W, H, levels, b4.element_size())
+    # one tensor per level (views of one buffer would turn in-place changes of
+    # a level into autograd errors)
     outs = [torch.empty((B, h, w, 4), dtype=b4.dtype, device=b4.device) for (w, h) in sizes[1:]]
     pipes, cmd = _objects(preset)
     lib = N.load()
     stream = torch.cuda.current_stream(b4.device).cuda_stream
     img = _image([b4.data_ptr()] + [o.data_ptr() for o in outs], W, H)
-    N.check(lib.nvproPyramidGenerateStrided(cmd.handle, stream, pipes.struct, _ptr(img),
-                                            _ptr(_strides(sizes, b4.element_size())), B, len(sizes)),
+    N.check(lib.nvproPyramidGenerateStrided(cmd.handle, stream, pipes.struct, _ptr(img), _ptr(strides), B,
+                                            len(sizes)),
             "nvproPyramidGenerateStrided")
     return outs
 
@@ -87,7 +105,7 @@ def adjoint(grads: list, shape, dtype, device, levels: int = 0) -> torch.Tensor:
     None), one strided nvproPyramidAdjoint call for the B images."""
     B, H, W, _ = shape
     preset = _PRESETS[dtype]
-    sizes = level_sizes(W, H, levels)
+    sizes = _geometry(W, H, levels, _ELEMENT_BYTES[dtype])[0]
     lib = N.load()
     stream = torch.cuda.current_stream(device).cuda_stream
     ws_bytes = lib.nvproPyramidAdjointWorkspaceBytes(W, H, len(sizes)) * B
