@@ -132,3 +132,32 @@ def test_read_tga_rle_bottom_up_24bit(native, repo_tmp):
     buf = np.empty(24, np.uint8)
     assert native.nvproPyramidReadTga(str(repo_tmp / "short.tga").encode(), buf.ctypes.data, 24, ctypes.byref(w),
                                       ctypes.byref(h)) == N.ERROR_IO
+
+
+@pytest.mark.parametrize("w,h", [(16384, 16384), (1920, 1080), (2052, 2052), (2048, 512), (4095, 4095), (64, 64),
+                                 (12, 8), (96, 40), (4096, 64)])
+def test_host_upload_band_plan(w, h):
+    """generate_from_host's plan: the first dispatch it bands is the default
+    schedule's first dispatch, and the band sub-images point at the rows of
+    every level the band's dispatch writes."""
+    from vk_compute_mipmaps_gb300 import pyramid as P
+    sched = O.default_schedule(w, h)
+    levels = O.full_levels(w, h)
+    n = P._first_fast_levels(w, h, levels)
+    first_fast, first_pc, _ = sched[0]
+    assert n == ((first_pc & 31) if first_fast else 0), (w, h)
+    if not n:
+        return
+    chain = P.MipChain(w, h, device="cpu")
+    base = chain.storage.data_ptr()
+    unit = 1 << n
+    rows = max(unit, (h // 4) // unit * unit)
+    for r0 in range(0, h, rows):
+        band = min(rows, h - r0)
+        img = P._sub_image(chain, 0, n + 1, r0, band)
+        assert (img.width, img.height, img.levelCount) == (w, band, n + 1)
+        for k in range(n + 1):
+            lw = max(w >> k, 1)
+            assert img.levels[k] == base + chain.offsets[k] + (r0 >> k) * lw * 4
+            assert img.rowPitchBytes[k] == lw * 4
+        assert r0 % unit == 0 and (band % unit == 0 or r0 + band == h)
