@@ -259,3 +259,53 @@ def test_premultiply_matches_reference_staging_golden():
     out = O.premultiply(img)
     assert np.array_equal(out[..., 3], img[..., 3])  # alpha unchanged
     assert np.array_equal(out[255], img[255]) and not out[0, :, :3].any()  # A = 255 keeps, A = 0 clears
+
+
+def numpy_blit(level: np.ndarray, dw: int, dh: int) -> np.ndarray:
+    """The pinned linear blit of the C ABI header, written independently in
+    numpy FP32 (decode with the oracle's tables, rows lerped first, each
+    operation rounded to FP32), for cross-checking the oracle's restatement."""
+    dec, alpha, _ = O.tables()
+    sh, sw = level.shape[:2]
+    lin = np.empty(level.shape, np.float32)
+    lin[..., :3] = dec[level[..., :3]]
+    lin[..., 3] = alpha[level[..., 3]]
+    f32 = np.float32
+
+    def axis(n_src, n_dst):
+        x = np.arange(n_dst, dtype=f32)
+        scale = f32(n_src) / f32(n_dst)
+        u = ((x + f32(0.5)).astype(f32) * scale).astype(f32) - f32(0.5)
+        u = u.astype(f32)
+        i = np.floor(u)
+        a = (u - i).astype(f32)
+        i = i.astype(np.int64)
+        return np.clip(i, 0, n_src - 1), np.clip(i + 1, 0, n_src - 1), a
+
+    x0, x1, ax = axis(sw, dw)
+    y0, y1, ay = axis(sh, dh)
+
+    def lerp(t0, t1, a):
+        b = (f32(1.0) - a).astype(f32)
+        return ((t0 * b[..., None]).astype(f32) + (t1 * a[..., None]).astype(f32)).astype(f32)
+
+    r0 = lerp(lin[y0][:, x0], lin[y0][:, x1], ax[None, :])
+    r1 = lerp(lin[y1][:, x0], lin[y1][:, x1], ax[None, :])
+    v = lerp(r0, r1, ay[:, None])
+    out = np.empty((dh, dw, 4), np.uint8)
+    out[..., :3] = O.srgb_encode_array(v[..., :3])
+    s = ((v[..., 3] * f32(255.0)).astype(f32) + f32(0.5)).astype(f32)
+    out[..., 3] = np.clip(np.floor(s), 0, 255).astype(np.uint8)
+    return out
+
+
+@pytest.mark.parametrize("w,h", [(5, 3), (9, 1), (1, 9), (37, 21), (64, 63), (255, 129)])
+def test_oracle_blit_matches_independent_restatement(w, h):
+    base = np.random.default_rng(w * h).integers(0, 256, (h, w, 4), dtype=np.uint8)
+    levels = O.full_levels(w, h)
+    buf = O.packed_from_base(1, base)
+    O.run(1, w, h, buf, [(2, 0 << 5 | 1, 1)])
+    off = O.offsets(w, h, levels, 4)
+    dw, dh = max(w >> 1, 1), max(h >> 1, 1)
+    got = buf[off[1]:off[2]].reshape(dh, dw, 4)
+    assert np.array_equal(got, numpy_blit(base, dw, dh))
