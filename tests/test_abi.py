@@ -247,3 +247,21 @@ def test_plain_c_caller(native, repo_tmp):
         got = [(2 if b else f, pc, g if (f or not b) else 1) for f, pc, g, b, _ in recs]
         assert got == [tuple(x) for x in want], (w, h, args)
         assert all(c == (fast_bits if f else general_bits) for f, _, _, b, c in recs if not b)
+
+
+def header_prototypes():
+    """name -> number of parameters, from every NVPRO_PYRAMID_API declaration."""
+    protos = {}
+    for hdr in (ROOT / "include").glob("*.h"):
+        src = re.sub(r"/\*.*?\*/", "", hdr.read_text(), flags=re.S)
+        for m in re.finditer(r"NVPRO_PYRAMID_API\s+[\w\s\*]+?\b(\w+)\s*\(([^;]*?)\)\s*;", src, flags=re.S):
+            params = m.group(2).strip()
+            protos[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return protos
+
+
+def test_python_signatures_match_header_arity(native):
+    protos = header_prototypes()
+    assert len(protos) >= 40
+    for name, n in protos.items():
+        assert len(N.SIGNATURES[name][1]) == n, (name, n, len(N.SIGNATURES[name][1]))
