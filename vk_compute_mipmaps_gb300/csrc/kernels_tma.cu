@@ -478,6 +478,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   __syncthreads();
   const Lut L = makeLut(lane);
+  // Programmatic dependent launch: everything above (tables, barriers) may
+  // overlap the end of the previous kernel on the stream; the first global
+  // access waits here until that kernel has completed and its writes are
+  // visible.  Then let the next kernel on the stream begin its own prologue
+  // as SMs free up.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
   const FusedStage& s0 = p.st[0];
   const uint32_t regions = s0.regionsX * s0.regionsY;
@@ -720,7 +727,17 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
   const uint64_t regions = uint64_t(tp.st[0].regionsX) * tp.st[0].regionsY;
   const uint32_t grid = uint32_t(std::min<uint64_t>(regions, uint64_t(info->sms)));
   void* args[] = {&map, &tp};
-  e = cudaLaunchKernel(tmaKernel(p.sharedFmt), dim3(grid), dim3(kThreads), args, kSmemBytes, stream);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = kSmemBytes;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;  // see griddepcontrol in the kernel
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelExC(&cfg, tmaKernel(p.sharedFmt), args);
   if (e != cudaSuccess) return e;
   ++*launches;
   return cudaGetLastError();
