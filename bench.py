@@ -23,6 +23,7 @@ import argparse
 import ctypes
 import json
 import os
+import socket
 import statistics
 import subprocess
 import sys
@@ -160,6 +161,19 @@ class Runner:
         return self.lib.nvproPyramidCmdLaunchCount(self.args[0])
 
 
+CLOCK_WINDOW_S = 0.6
+
+
+def keep_busy(fn, seconds):
+    """Run `fn` back to back (untimed) for about `seconds` of wall time."""
+    import torch
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for _ in range(8):
+            fn()
+        torch.cuda.synchronize()
+
+
 def time_loop(fn, stream, steps, warmup, flush=None):
     """Per-step device times (ms) with CUDA events on `stream`."""
     import torch
@@ -231,26 +245,34 @@ def bench_premultiply(dev, stream, steps, w=16384, h=16384):
             "frac_of_hbm_peak": round(nbytes / (us * 1e-6) / 1e9 / peak, 4), "bytes": nbytes}
 
 
-def bench_batch(dev, stream, flush, steps):
+def bench_batch(dev, stream, flush, steps, rank=0, world=1):
     """256 sRGBA8 images (sides log-uniform in [17, 4096], aspect in [1/4, 4],
     seed 2024) in one buffer: one batch launch (autotuned, CUDA graph) against
-    256 per-image nvproPyramidGenerate calls, both device-timed, L2 flushed."""
+    256 per-image nvproPyramidGenerate calls, both device-timed, L2 flushed.
+    With several ranks the 256 images are split by image (shard_by_image):
+    each rank launches a batch of its share, and the job's time is the max
+    over ranks (no data is exchanged)."""
     import torch
     import vk_compute_mipmaps_gb300 as V
-    from vk_compute_mipmaps_gb300.workloads import batch_sizes, chain_bytes
+    from vk_compute_mipmaps_gb300.workloads import batch_sizes, chain_bytes, shard_by_image
     peak, _ = measured_peak()
-    sizes = batch_sizes(256)
+    all_sizes = batch_sizes(256)
+    sizes = [all_sizes[i] for i in shard_by_image(all_sizes, rank, world)]
     storage, chains = V.pack_chains(sizes, device=dev)
     g = torch.Generator(device=dev).manual_seed(2024)
     storage.copy_(torch.randint(0, 256, (storage.numel(),), generator=g, device=dev, dtype=torch.uint8))
-    nbytes = sum(chain_bytes(w, h) for w, h in sizes)
+    nbytes = sum(chain_bytes(w, h) for w, h in all_sizes)
     with torch.cuda.stream(stream):
         batch = V.Batch(V.BATCH_AUTOTUNE | V.BATCH_GRAPH)
         batch.build(chains, stream=stream.cuda_stream)
+        barrier(world)
         tb = time_loop(lambda: batch.launch(stream.cuda_stream), stream, steps, 3, flush=flush)
+        barrier(world)
         tp = time_loop(lambda: [V.generate(c, stream=stream.cuda_stream) for c in chains], stream,
                        max(3, steps // 4), 3, flush=flush)
-    b_us, p_us = statistics.median(tb) * 1e3, statistics.median(tp) * 1e3
+    b_us = max_over_ranks(statistics.median(tb) * 1e3, world)
+    p_us = max_over_ranks(statistics.median(tp) * 1e3, world)
+    sizes = all_sizes
     info = batch.info()
     batch.close()
     del storage, chains
@@ -261,7 +283,8 @@ def bench_batch(dev, stream, flush, steps):
             "speedup_vs_plain": round(p_us / b_us, 3), "algorithmic_bytes": nbytes,
             "batch_frac_of_hbm_peak": round(nbytes / (b_us * 1e-6) / 1e9 / peak, 4),
             "phases": info["phaseCount"], "jobs": info["jobCount"], "strip_band": info["stripBand"],
-            "launches_per_batch": 1}
+            "launches_per_batch": 1, "ranks": world,
+            "split": "by image across ranks, max of the ranks' times" if world > 1 else "one GPU"}
 
 
 def level_errors_fp64(levels, base):
@@ -493,15 +516,21 @@ def run_ours(args, rank, world):
         for _ in range(args.warmup):
             run()
         torch.cuda.synchronize()
-        barrier(world)
         launches = 0
+        # nvidia-smi samples every 100 ms, longer than the timed steps take:
+        # the sampler runs over untimed chains for CLOCK_WINDOW_S before and
+        # after the timed steps, the same load, so the clocks are those the
+        # timed steps ran at.
         with ClockSampler(dev) as clk:
+            keep_busy(run, CLOCK_WINDOW_S)
+            barrier(world)
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
             for _ in range(args.steps):
                 launches += run()
             e.record(stream)
             torch.cuda.synchronize()
+            keep_busy(run, CLOCK_WINDOW_S)
         ms = s.elapsed_time(e)
     ms = max_over_ranks(ms, world)
     ms_per_step = ms / args.steps
@@ -555,18 +584,19 @@ def run_ours(args, rank, world):
         e2e = {"value": round(e2e_us, 2), "unit": "us", "h2d_bytes_per_step": base_host.numel(),
                "d2h_bytes_per_step": out_host.numel(), "steps": n_e2e}
         del base_host, out_host
+    if not args.no_extra:  # every rank: its share of the batch
+        flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+        del chain
+        torch.cuda.empty_cache()
+        extra["batch_256"] = bench_batch(dev, stream, flush, max(5, min(args.steps, 20)), rank, world)
     if rank == 0:
         if not args.no_extra:
-            flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-            del chain
-            torch.cuda.empty_cache()
             for cw, ch in CONFIGS:
                 # 2048^2: uniform random bytes; the others: a smooth seeded field with radial alpha
                 content = "random" if (cw, ch) == (2048, 2048) else "smooth"
                 extra[f"{cw}x{ch}"] = bench_config(cw, ch, dev, stream, flush, max(10, min(args.steps, 100)),
                                                    content)
                 extra[f"{cw}x{ch}"]["content"] = content
-            extra["batch_256"] = bench_batch(dev, stream, flush, max(5, min(args.steps, 20)))
             extra["premultiply_staging"] = bench_premultiply(dev, stream, max(5, min(args.steps, 20)))
             extra["float_adjoint"] = bench_float_adjoint(dev, stream, flush, max(5, min(args.steps, 20)))
             del flush
@@ -726,6 +756,16 @@ def main(argv=None):
     if args.profile:
         run_profile(args.profile, args.steps)
         return
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # No launcher: start one rank per GPU (replicas, see run_ours) the way
+        # the multi-GPU contract does, on this host.
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()),
+               *(sys.argv[1:] if argv is None else argv)]
+        raise SystemExit(subprocess.call(cmd))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

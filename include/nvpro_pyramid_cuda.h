@@ -273,7 +273,12 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidPremultiplyAlpha(
  * completes; 1: the general chain's grid barrier that nothing releases.  It
  * gives up after its limit (about a second) and sets the command's error
  * flag, so the next nvproPyramidCmdDeviceStatus reports
- * NVPRO_PYRAMID_ERROR_TIMEOUT and resets the counters; nothing faults. */
+ * NVPRO_PYRAMID_ERROR_TIMEOUT and resets the counters; nothing faults.
+ * waitKind 2 launches nothing: in the command's next TMA fast-kernel launch,
+ * CTA 0 takes the path of a wait that gave up at once (its regions stay
+ * unwritten, the fused tail is skipped, the error flag is set) while the
+ * kernel's own counter still returns to zero, so later launches are correct
+ * before any status query. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugForceWaitTimeout(NvproPyramidCmd cmd, uint32_t waitKind);
 
 /* Test support (no reference counterpart): encode n floats of x (device
@@ -412,21 +417,38 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidAdjointStrided(
  * application owns every device allocation (plugins, fixed memory budgets),
  * and hot loops that must not call cudaMalloc/cudaFree (cudaFree synchronises
  * the device).  nvproPyramidCreateCmd allocates a few bytes of device counters;
- * this entry point instead uses a fixed 256-byte __device__ array of the
- * library (64 words: two per TMA launch and four per run of general
- * dispatches of the chain, more than any chain needs; a chain that needed
- * more would be rejected with NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT).  Every GPU that loads the library
- * holds the array until the process exits.
+ * this entry point instead uses a fixed 1 KiB __device__ array of the library
+ * (256 words: one error word, then two per TMA launch and five per run of
+ * general dispatches of the chain; a chain has at most 31 dispatches, so every
+ * chain fits, and the words a chain needs are checked before anything is
+ * enqueued).  Every GPU that loads the library holds the array until the
+ * process exits.
  *
- * The first call on a device looks up the array's device address
+ * The first call on a device (and again after the device's context was made
+ * anew, e.g. after cudaDeviceReset) looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
  * before any stream capture.  All calls share the array and it keeps the last
- * call's contents; each call clears it on `stream` first.  Calls whose work
- * overlaps on the GPU (e.g. on two streams without ordering) race on it:
- * order them. */
+ * call's contents: each call clears its launch counters on `stream` first,
+ * while the error word keeps a timed-out wait of any call until
+ * nvproPyramidNoAllocDeviceStatus reads it.  Calls whose work overlaps on the
+ * GPU (e.g. on two streams without ordering) race on the array: order them. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidGenerateNoAlloc(
     NvproPyramidStream stream, NvproPyramidPreset preset, const NvproPyramidImage* pImage,
     uint32_t mipLevels);
+
+/* The device status of nvproPyramidGenerateNoAlloc, allocating nothing (the
+ * no-allocation counterpart of nvproPyramidCmdDeviceStatus): wait for
+ * `stream`, then report NVPRO_PYRAMID_ERROR_TIMEOUT if a bounded device-side
+ * wait of a kernel launched by nvproPyramidGenerateNoAlloc (on any stream of
+ * the current device) gave up since the last query -- the outputs of that call
+ * are then incomplete -- and clear the report. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidNoAllocDeviceStatus(NvproPyramidStream stream);
+
+/* Test support (no reference counterpart): nvproPyramidDebugForceWaitTimeout
+ * on the fixed array of nvproPyramidGenerateNoAlloc, on `stream`: the next
+ * nvproPyramidNoAllocDeviceStatus reports NVPRO_PYRAMID_ERROR_TIMEOUT. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugNoAllocForceWaitTimeout(NvproPyramidStream stream,
+                                                                             uint32_t waitKind);
 
 /* ------------------------------------------------------------------------ */
 /* Batches (no reference counterpart: the reference records one chain per   */

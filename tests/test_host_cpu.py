@@ -42,6 +42,69 @@ def test_bench_rank_helpers_gloo_world_2():
         assert dict(out) == {0: 11.5, 1: 11.5}
 
 
+def _shard_rank_main(rank, world, port, out):
+    import hashlib
+
+    import torch.distributed as dist
+
+    from vk_compute_mipmaps_gb300.workloads import shard_by_image
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sizes = batch_sizes(24, seed=9, lo=3, hi=96)
+        rng = np.random.default_rng(31)
+        bases = [rng.integers(0, 256, (h, w, 4), dtype=np.uint8) for w, h in sizes]
+
+        def digest(i):  # the pyramid of image i (the oracle stands in for a GPU)
+            return hashlib.sha256(O.pyramid(1, bases[i]).tobytes()).hexdigest()
+
+        mine = shard_by_image(sizes, rank, world)
+        gathered = [None] * world
+        dist.all_gather_object(gathered, {i: digest(i) for i in mine})
+        if rank == 0:
+            out["shares"] = [sorted(g) for g in gathered]
+            out["merged"] = {k: v for g in gathered for k, v in g.items()}
+            out["single"] = {i: digest(i) for i in range(len(sizes))}
+            out["bytes"] = [sum(chain_bytes(*sizes[i]) for i in g) for g in gathered]
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_batch_split_by_image_gloo_world_2():
+    """Two ranks split a batch by image with no exchange: the shares are
+    disjoint, cover every image, carry about the same bytes, and each rank's
+    pyramids equal those of one process generating the whole batch."""
+    import torch.multiprocessing as mp
+    world, port = 2, _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_shard_rank_main, args=(world, port, out), nprocs=world, join=True)
+        shares = out["shares"]
+        assert sorted(shares[0] + shares[1]) == list(range(24)) and not set(shares[0]) & set(shares[1])
+        assert out["merged"] == out["single"]
+        b0, b1 = out["bytes"]
+        assert abs(b0 - b1) <= max(b0, b1) * 0.25
+
+
+def test_bench_gpus_flag_launches_ranks():
+    """`bench.py --gpus 2` without a launcher starts two ranks itself; the
+    CPU reference arm then prints one line with n_gpus 2 from rank 0."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    res = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference", "--gpus", "2",
+                          "--steps", "1", "--warmup", "0"], capture_output=True, text=True, env=env, timeout=600,
+                         cwd=root)
+    assert res.returncode == 0, res.stderr[-2000:]
+    lines = [json.loads(ln) for ln in res.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, res.stdout
+    assert lines[0]["n_gpus"] == 2 and lines[0]["impl"] == "reference"
+
+
 def test_batch_workload_is_seeded_and_mixed():
     a, b = batch_sizes(256), batch_sizes(256)
     assert a == b and len(a) == 256

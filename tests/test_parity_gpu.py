@@ -248,12 +248,10 @@ def test_pitched_separate_levels(cuda, w, h):
             assert np.array_equal(got, want[off[k]:off[k + 1]]), (flags, k)
 
 
-def test_16384_chain_tile_local_and_tail(cuda):
-    """The 16384^2 benchmark chain (F6, F6, F2) at full size, through
-    size-independent properties: every 64x64 tile of level 0 determines its
-    levels 1..6 alone (checked on random tiles against the oracle), the top
-    levels 7..14 follow from level 6 alone (checked against the oracle run on
-    the GPU's level 6), and all kernel paths write identical bytes."""
+def test_16384_chain_bit_exact(cuda):
+    """The 16384^2 benchmark chain (schedule F6, F6, F2; seeded uniform random
+    bytes as in the bench) at full size: all 15 levels byte for byte against
+    the oracle, and identical bytes from every kernel path."""
     import torch
     w = h = 16384
     g = torch.Generator(device=cuda).manual_seed(1234)
@@ -261,27 +259,71 @@ def test_16384_chain_tile_local_and_tail(cuda):
     chain.storage.fill_(SENTINEL)
     chain.storage[:chain.offsets[1]].copy_(
         torch.randint(0, 256, (chain.offsets[1],), generator=g, device=cuda, dtype=torch.uint8))
-    results = []
+    base = chain.level(0).cpu().numpy()
+    want = O.pyramid(1, base)
+    mips = chain.levels
+    first = None
     for flags in FLAGS:
         chain.storage[chain.offsets[1]:].fill_(SENTINEL)
         P.generate(chain, flags=flags)
         torch.cuda.synchronize()
-        results.append(chain.storage[chain.offsets[1]:].clone())
-    for r in results[1:]:
-        assert torch.equal(results[0], r)
-    rng = np.random.default_rng(5)
-    for _ in range(12):
-        tx, ty = rng.integers(0, 256, 2)
-        tile = chain.level(0)[ty * 64:(ty + 1) * 64, tx * 64:(tx + 1) * 64].cpu().numpy()
-        want = O.split_levels(O.pyramid(1, tile, schedule=[(1, 6, 1)], mips=7), 64, 64, 7, 4, np.uint8)
-        for k in range(1, 7):
-            e = 64 >> k
-            got = chain.level(k)[ty * e:(ty + 1) * e, tx * e:(tx + 1) * e].cpu().numpy()
-            assert np.array_equal(got, want[k]), (tx, ty, k)
-    lvl6 = chain.level(6).cpu().numpy()
-    want = O.split_levels(O.pyramid(1, lvl6), 256, 256, 9, 4, np.uint8)
-    for k in range(1, 9):
-        assert np.array_equal(chain.level(6 + k).cpu().numpy(), want[k]), k
+        got = chain.storage.cpu().numpy()
+        assert_same(got, want, w, h, 4, mips, f"16384^2 flags={flags}")
+        if first is None:
+            first = got
+        else:
+            assert np.array_equal(first, got), flags
+
+
+def test_16384_chain_srgb_shared_bit_exact(cuda):
+    """16384^2 with SRGB_SHARED pipelines (the F6 dispatches hand level L+4 on
+    as sRGBA8 codes) against the oracle's shared-format mode, all levels."""
+    import torch
+    w = h = 16384
+    g = torch.Generator(device=cuda).manual_seed(4321)
+    chain = P.MipChain(w, h, N.PRESET_SRGBA8, device=cuda)
+    chain.storage.fill_(SENTINEL)
+    chain.storage[:chain.offsets[1]].copy_(
+        torch.randint(0, 256, (chain.offsets[1],), generator=g, device=cuda, dtype=torch.uint8))
+    base = chain.level(0).cpu().numpy()
+    pipes = P.Pipelines(N.PRESET_SRGBA8, general_config=N.CONFIG_SRGB_SHARED, fast_config=N.CONFIG_SRGB_SHARED)
+    P.generate(chain, pipelines=pipes, cmd=P.Cmd(0))
+    torch.cuda.synchronize()
+    want = O.pyramid(1, base, fast_shared=O.SHARED_SRGB, general_shared=O.SHARED_SRGB)
+    assert_same(chain.storage.cpu().numpy(), want, w, h, 4, chain.levels, "16384^2 SRGB_SHARED")
+
+
+def test_back_to_back_chains_across_the_programmatic_launch_edge(cuda):
+    """Two chains on one stream with no synchronisation between them, the
+    second reading the first's output: chain B's level 0 is chain A's level 1
+    (a view, no copy).  The fast kernel starts as a programmatic dependent
+    launch and waits for the previous kernel before its first global access,
+    so B sees A's finished level 1."""
+    import torch
+    wa = ha = 4096
+    base = random_base(N.PRESET_SRGBA8, wa, ha, 77)
+    a = P.MipChain(wa, ha, N.PRESET_SRGBA8, device=cuda)
+    a.storage.fill_(SENTINEL)
+    a.level(0).copy_(torch.from_numpy(base))
+    wb, hb = wa // 2, ha // 2
+    b = P.MipChain(wb, hb, N.PRESET_SRGBA8, device=cuda)
+    b.storage.fill_(SENTINEL)
+    b_img = P.make_image([a.storage.data_ptr() + a.offsets[1]] +
+                         [b.storage.data_ptr() + o for o in b.offsets[1:-1]], wb, hb)
+    lib = N.load()
+    pipes, cmd_a, cmd_b = P.Pipelines(N.PRESET_SRGBA8), P.Cmd(0), P.Cmd(0)
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    for _ in range(3):  # repeated: A rewrites its level 1 while B's previous launch is done
+        N.check(lib.nvproPyramidGenerate(cmd_a.handle, stream, pipes.struct, ctypes.byref(a.image()), 0), "A")
+        N.check(lib.nvproPyramidGenerate(cmd_b.handle, stream, pipes.struct, ctypes.byref(b_img), 0), "B")
+    torch.cuda.synchronize()
+    want_a = O.pyramid(1, base)
+    assert np.array_equal(a.storage.cpu().numpy(), want_a)
+    lvl1 = O.split_levels(want_a, wa, ha, P.full_level_count(wa, ha), 4, np.uint8)[1]
+    want_b = O.pyramid(1, lvl1)
+    got_b = b.storage.cpu().numpy()
+    off = O.offsets(wb, hb, P.full_level_count(wb, hb), 4)
+    assert np.array_equal(got_b[off[1]:], want_b[off[1]:])
 
 
 def test_fast_srgb_encoder_exhaustive(cuda, native):

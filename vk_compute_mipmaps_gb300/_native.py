@@ -157,6 +157,8 @@ SIGNATURES = {
     "nvproPyramidAdjoint": (c_int, [c_void_p, c_int, POINTER(NvproPyramidImage), c_void_p, c_uint64, c_uint32,
                                     c_void_p, c_uint64]),
     "nvproPyramidGenerateNoAlloc": (c_int, [c_void_p, c_int, POINTER(NvproPyramidImage), c_uint32]),
+    "nvproPyramidNoAllocDeviceStatus": (c_int, [c_void_p]),
+    "nvproPyramidDebugNoAllocForceWaitTimeout": (c_int, [c_void_p, c_uint32]),
     # image / stride arrays by address (the autograd helpers pass numpy buffers)
     "nvproPyramidGenerateStrided": (c_int, [c_void_p, c_void_p, NvproPyramidPipelines, c_void_p, c_void_p, c_uint32,
                                             c_uint32]),

@@ -81,6 +81,8 @@ struct NvproPyramidCmd_T {
   // set by nvproPyramidGenerateStrided for the duration of one EndCmd
   uint32_t batch = 1;
   uint64_t imageStrides[NVPRO_PYRAMID_MAX_LEVELS] = {};
+  // nvproPyramidDebugForceWaitTimeout(cmd, 2): CTA 0 of the next TMA launch gives up at once
+  bool debugFailNextTma = false;
 };
 
 namespace {
@@ -451,7 +453,8 @@ NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
         tail = j - i - 1;
       }
       e = launchTmaFast(p, tail ? &params[i + 1] : nullptr, uint32_t(tail), cmd->stream, cmd->scratch,
-                        &cmd->launches);
+                        &cmd->launches, cmd->debugFailNextTma ? 0u : ~0u);
+      cmd->debugFailNextTma = false;
       i += 1 + tail;
     } else if (!portableOnly && generalFastSupported(p)) {
       // A run of general dispatches is one launch (fused unless NO_FUSION).
@@ -624,10 +627,13 @@ NvproPyramidResult nvproPyramidDebugForceWaitTimeout(NvproPyramidCmd cmd, uint32
   if (!cmd->scratch.counters) return fail(NVPRO_PYRAMID_ERROR_INVALID_STATE, "command without device counters");
   cudaError_t e;
   if (waitKind == 0)
-    e = launchDebugMbarTimeout(cmd->scratch.counters + kCounterError, cmd->stream);
+    e = launchDebugMbarTimeout(cmd->scratch.error(), cmd->stream);
   else if (waitKind == 1)
     e = launchDebugGridBarrierTimeout(cmd->scratch, cmd->stream);
-  else
+  else if (waitKind == 2) {
+    cmd->debugFailNextTma = true;
+    e = cudaSuccess;
+  } else
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "waitKind %u", waitKind);
   if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "launch failed: %s", cudaGetErrorString(e));
   return NVPRO_PYRAMID_SUCCESS;
@@ -957,43 +963,89 @@ NvproPyramidResult nvproPyramidGenerateNoAlloc(NvproPyramidStream stream, NvproP
   if (r != NVPRO_PYRAMID_SUCCESS) return r;
   if (count == 0) return NVPRO_PYRAMID_SUCCESS;
 
+  // Plan every launch and its words of the fixed array before enqueueing
+  // anything, so a rejected chain leaves the stream untouched.
+  struct Launch {
+    uint32_t kind;  // 0 TMA fast kernel (+ fused tail), 1 general chain, 2 portable
+    uint32_t first, count, word;
+  };
+  Launch plan[NVPRO_PYRAMID_MAX_LEVELS];
+  uint32_t launchCount = 0, words = kStaticErrorWord + 1;
+  for (uint32_t i = 0; i < count;) {
+    const DispatchParams& p = params[i];
+    Launch& l = plan[launchCount++];
+    l.first = i;
+    l.word = words;
+    uint32_t j = i + 1;
+    if (p.isFast && tmaFastSupported(p)) {
+      while (j < count && j - i < tmaMaxFused() && tmaTailCompatible(params[j - 1], params[j])) ++j;
+      l.kind = 0;
+      words += kTmaScratchWords;
+    } else if (generalFastSupported(p)) {
+      while (j < count && j - i < generalMaxStages() && generalFastSupported(params[j])) ++j;
+      l.kind = 1;
+      words += kGeneralScratchWords;
+    } else {
+      l.kind = 2;
+    }
+    l.count = j - i;
+    i = j;
+  }
+  if (words > kStaticScratchWords)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "chain needs %u of the %u fixed scratch words", words,
+                kStaticScratchWords);
+
   uint32_t* scratch = nullptr;
   const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   cudaError_t e = staticScratch(&scratch);
-  // Calls share the array and it keeps the last call's contents: start from zero.
-  if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, kStaticScratchWords * sizeof(uint32_t), s);
+  // Calls share the array and it keeps the last call's contents: the counters
+  // start from zero; the error word stays until the status query reads it.
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(scratch + kStaticErrorWord + 1, 0, (words - kStaticErrorWord - 1) * sizeof(uint32_t), s);
   if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "static scratch: %s", cudaGetErrorString(e));
-  // Each launch that needs scratch gets its own words of the fixed array:
-  // 2 per TMA launch (last-CTA counter, error flag), 4 per general chain.
-  uint32_t launches = 0, used = 0;
-  uint32_t i = 0;
-  while (i < count) {
-    const DispatchParams& p = params[i];
-    if (p.isFast && tmaFastSupported(p)) {
-      uint32_t j = i + 1;
-      while (j < count && j - i < tmaMaxFused() && tmaTailCompatible(params[j - 1], params[j])) ++j;
-      if (used + 2 > kStaticScratchWords)
-        return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "chain needs more than the %u fixed scratch words",
-                    kStaticScratchWords);
-      const Scratch sc{scratch + used, 2};
-      e = launchTmaFast(p, j > i + 1 ? &params[i + 1] : nullptr, j - i - 1, s, sc, &launches);
-      used += 2;
-      i = j;
-    } else if (generalFastSupported(p)) {
-      uint32_t j = i + 1;
-      while (j < count && j - i < generalMaxStages() && generalFastSupported(params[j])) ++j;
-      if (used + kCounterBarrierGen + 1 > kStaticScratchWords)
-        return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "chain needs more than the %u fixed scratch words",
-                    kStaticScratchWords);
-      e = launchGeneralChain(&params[i], j - i, s, Scratch{scratch + used, kCounterBarrierGen + 1}, &launches);
-      used += kCounterBarrierGen + 1;
-      i = j;
-    } else {
+  uint32_t launches = 0;
+  for (uint32_t k = 0; k < launchCount && e == cudaSuccess; ++k) {
+    const Launch& l = plan[k];
+    const DispatchParams& p = params[l.first];
+    if (l.kind == 0)
+      e = launchTmaFast(p, l.count > 1 ? &p + 1 : nullptr, l.count - 1, s,
+                        Scratch{scratch + l.word, kTmaScratchWords, scratch + kStaticErrorWord}, &launches);
+    else if (l.kind == 1)
+      e = launchGeneralChain(&p, l.count, s,
+                             Scratch{scratch + l.word, kGeneralScratchWords, scratch + kStaticErrorWord}, &launches);
+    else
       e = launchPortable(p, s, &launches);
-      ++i;
-    }
-    if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
   }
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidNoAllocDeviceStatus(NvproPyramidStream stream) {
+  uint32_t* scratch = nullptr;
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  cudaError_t e = staticScratch(&scratch);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  uint32_t flag = 0;  // read into the stack: nothing is allocated
+  if (e == cudaSuccess) e = cudaMemcpy(&flag, scratch + kStaticErrorWord, sizeof flag, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && flag) {
+    e = cudaMemsetAsync(scratch + kStaticErrorWord, 0, sizeof flag, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "no-alloc device status: %s", cudaGetErrorString(e));
+  if (flag) return fail(NVPRO_PYRAMID_ERROR_TIMEOUT, "a device-side wait gave up; outputs are incomplete");
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidDebugNoAllocForceWaitTimeout(NvproPyramidStream stream, uint32_t waitKind) {
+  if (waitKind > 1) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "waitKind %u", waitKind);
+  uint32_t* scratch = nullptr;
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  cudaError_t e = staticScratch(&scratch);
+  // the counters of a general launch at the first per-launch word, the error word shared
+  const Scratch sc{scratch + kStaticErrorWord + 1, kGeneralScratchWords, scratch + kStaticErrorWord};
+  if (e == cudaSuccess && waitKind == 1) e = cudaMemsetAsync(sc.counters, 0, kGeneralScratchWords * 4, s);
+  if (e == cudaSuccess) e = waitKind == 0 ? launchDebugMbarTimeout(sc.error(), s) : launchDebugGridBarrierTimeout(sc, s);
+  if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "launch failed: %s", cudaGetErrorString(e));
   return NVPRO_PYRAMID_SUCCESS;
 }
 

@@ -52,10 +52,21 @@ struct DispatchParams {
   uint64_t imageStride[kMaxDispatchLevels + 1] = {};
 };
 
-// Device scratch owned by a command object (allocated at creation).
+// Scratch counter slots.
+constexpr uint32_t kCounterLastCta = 0;
+constexpr uint32_t kCounterError = 1;
+constexpr uint32_t kCounterBarrier = 2;     // general chain: CTAs arrived at the barrier
+constexpr uint32_t kCounterBarrierGen = 3;  // general chain: barrier generation
+constexpr uint32_t kCounterExit = 4;        // general chain: CTAs that have exited (repairs the barrier count)
+
+// Device scratch of a launch: counter words owned by a command object
+// (allocated at creation) or a slice of the fixed no-allocation array.
 struct Scratch {
   uint32_t* counters;     // zero-initialised, self-resetting
   uint32_t counterCount;
+  // Where a bounded wait that gives up records it; null: counters + kCounterError.
+  uint32_t* errorFlag = nullptr;
+  uint32_t* error() const { return errorFlag ? errorFlag : counters + kCounterError; }
 };
 
 // Kernel families.  Each returns cudaSuccess or the launch error, and adds the
@@ -67,8 +78,11 @@ bool tmaFastSupported(const DispatchParams& p);
 bool tmaTailCompatible(const DispatchParams& prev, const DispatchParams& next);
 // Maximum number of dispatches one TMA launch runs (itself plus its tail).
 uint32_t tmaMaxFused();
+// debugFailCta (test support): that CTA gives up at once, as after a wait
+// that ran out; ~0u = none.
 cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, uint32_t tailCount,
-                          cudaStream_t stream, const Scratch& scratch, uint32_t* launches);
+                          cudaStream_t stream, const Scratch& scratch, uint32_t* launches,
+                          uint32_t debugFailCta = ~0u);
 // Test support: the fast sRGB encoder and the exact threshold count, per float.
 cudaError_t launchDebugEncode(const float* x, uint8_t* fast, uint8_t* exact, uint64_t n, uint32_t alpha,
                               cudaStream_t stream);
@@ -111,7 +125,8 @@ struct AdjointLevelParams {
 // least 2x2 (and level L+1 too, for 2 levels) with full workgroup coverage.
 // A run of up to generalMaxStages() such dispatches is one cooperative launch
 // with grid barriers between them; for more than one dispatch it uses scratch
-// words kCounterError, kCounterBarrier and kCounterBarrierGen.
+// words kCounterError (or scratch.errorFlag), kCounterBarrier,
+// kCounterBarrierGen and kCounterExit.
 bool generalFastSupported(const DispatchParams& p);
 uint32_t generalMaxStages();
 cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStream_t stream, const Scratch& scratch,
@@ -127,24 +142,31 @@ cudaError_t launchProbe(const uint8_t* const* levels, const uint64_t* pitches, u
 
 // Test support for failure detection: a bounded wait that runs out (an
 // mbarrier phase nothing completes; a grid barrier nothing releases) and
-// sets the error flag of `scratch` / errorFlag.
+// sets the error flag of `scratch` (scratch.error()) / errorFlag.
 cudaError_t launchDebugMbarTimeout(uint32_t* errorFlag, cudaStream_t stream);
 cudaError_t launchDebugGridBarrierTimeout(const Scratch& scratch, cudaStream_t stream);
 
 cudaError_t launchAdjointChain(const AdjointChainParams& p, cudaStream_t stream);
 cudaError_t launchAdjointLevel(const AdjointLevelParams& p, cudaStream_t stream);
 
-// Scratch counter slots.
-constexpr uint32_t kCounterLastCta = 0;
-constexpr uint32_t kCounterError = 1;
-constexpr uint32_t kCounterBarrier = 2;     // general chain: CTAs arrived at the barrier
-constexpr uint32_t kCounterBarrierGen = 3;  // general chain: barrier generation
+// Words a launch uses: TMA fast kernel (last-CTA counter, error flag) and a
+// general chain of two or more stages (error flag, barrier count, generation,
+// exit count; slot 0 unused).
+constexpr uint32_t kTmaScratchWords = kCounterError + 1;
+constexpr uint32_t kGeneralScratchWords = kCounterExit + 1;
 
 // The fixed device scratch of nvproPyramidGenerateNoAlloc: kStaticScratchWords
-// words in a file-scope __device__ array.  Returns its device address for the
-// current device, doing the per-device look-up (cudaGetSymbolAddress) on first
-// use.
-constexpr uint32_t kStaticScratchWords = 64;
+// words in a file-scope __device__ array.  Word kStaticErrorWord is the error
+// flag of every launch of that path (kept until nvproPyramidNoAllocDeviceStatus
+// reads and clears it); the words after it are the per-launch counters, which
+// each call clears.  A chain has at most NVPRO_PYRAMID_MAX_LEVELS - 1
+// dispatches, each launch covers at least one, and no launch needs more than
+// kGeneralScratchWords words, so every chain fits.  Returns the array's device
+// address for the current device and context, looked up (cudaGetSymbolAddress)
+// on first use there.
+constexpr uint32_t kStaticScratchWords = 256;
+constexpr uint32_t kStaticErrorWord = 0;
+static_assert(kStaticScratchWords >= 1 + 31 * kGeneralScratchWords, "a chain's launches must fit the fixed array");
 cudaError_t staticScratch(uint32_t** ptr);
 
 // Set the calling thread's nvproPyramidLastError text.

@@ -32,6 +32,7 @@ struct ChainParams {
   uint32_t* barrierCount;  // CTAs arrived at the current barrier (self-resetting)
   uint32_t* barrierGen;    // barrier generation (only ever incremented)
   uint32_t* errorFlag;     // set to 1 if a bounded wait gave up
+  uint32_t* exitCount;     // CTAs that have left (self-resetting; see exitArrive)
 };
 
 __device__ __forceinline__ bool gridBarrier(const ChainParams& p, uint32_t& gen, uint32_t* okFlag) {
@@ -43,6 +44,22 @@ __device__ __forceinline__ void runStage(const Stage& st, uint32_t lane, uint32_
   const uint32_t units = st.tilesX * st.bands;
   for (uint32_t u = warpId; u < units; u += warps)
     strip<SF, kRuntimeVariant, ROWS>(st, u % st.tilesX, u / st.tilesX, lane, L);
+}
+
+// Every CTA of a multi-stage launch arrives here once on its way out.  The
+// last one resets the barrier count: after a bounded wait gave up, CTAs leave
+// at different barriers and the count can be left partial; the reset puts it
+// back to zero for the next launch (no CTA uses it any more).
+__device__ __forceinline__ void exitArrive(const ChainParams& p) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(p.exitCount, 1u) == gridDim.x - 1) {
+      atomicExch(p.barrierCount, 0u);
+      atomicExch(p.exitCount, 0u);
+      __threadfence();
+    }
+  }
 }
 
 // SF: the general pipeline's shared format (one per launch); ROWS: the strip's
@@ -64,13 +81,14 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
     runStage<SF, ROWS>(p.st[s], lane, alone ? localWarp : warpId, alone ? kWarps : warps, L);
     if (s + 1 == p.stageCount) break;
     if (s + 1 < p.tailFrom) {
-      if (!gridBarrier(p, gen, &okFlag)) return;
+      if (!gridBarrier(p, gen, &okFlag)) break;
     } else if (s + 1 == p.tailFrom) {
-      if (!lastCtaArrives(p.barrierCount, &okFlag)) return;  // the others are done
+      if (!lastCtaArrives(p.barrierCount, &okFlag)) break;  // the others are done
     } else {
       __syncthreads();  // the small stages: one CTA, block-level order
     }
   }
+  if (p.stageCount > 1) exitArrive(p);
 }
 
 // Test support for failure detection: one CTA arrives at the chain kernels'
@@ -163,16 +181,15 @@ bool generalFastSupported(const DispatchParams& p) {
 uint32_t generalMaxStages() { return kMaxStages; }
 
 cudaError_t launchDebugGridBarrierTimeout(const Scratch& scratch, cudaStream_t stream) {
-  if (scratch.counterCount <= kCounterBarrierGen) return cudaErrorInvalidValue;
+  if (scratch.counterCount < kGeneralScratchWords) return cudaErrorInvalidValue;
   debugGridBarrierTimeoutKernel<<<1, 32, 0, stream>>>(scratch.counters + kCounterBarrier,
-                                                       scratch.counters + kCounterBarrierGen,
-                                                       scratch.counters + kCounterError);
+                                                       scratch.counters + kCounterBarrierGen, scratch.error());
   return cudaGetLastError();
 }
 
 cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStream_t stream, const Scratch& scratch,
                                uint32_t* launches) {
-  if (count == 0 || count > kMaxStages || (count > 1 && scratch.counterCount <= kCounterBarrierGen))
+  if (count == 0 || count > kMaxStages || (count > 1 && scratch.counterCount < kGeneralScratchWords))
     return cudaErrorInvalidValue;
   for (uint32_t i = 1; i < count; ++i)
     if (p[i].sharedFmt != p[0].sharedFmt) return cudaErrorInvalidValue;  // one shared format per launch
@@ -199,7 +216,8 @@ cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStre
   if (count > 1) {
     cp.barrierCount = scratch.counters + kCounterBarrier;
     cp.barrierGen = scratch.counters + kCounterBarrierGen;
-    cp.errorFlag = scratch.counters + kCounterError;
+    cp.errorFlag = scratch.error();
+    cp.exitCount = scratch.counters + kCounterExit;
   }
   // a single stage needs no more CTAs than its strips fill; small stages only: one
   uint32_t grid = count > 1 ? ctas : uint32_t(std::min<uint64_t>((maxUnits + kWarps - 1) / kWarps, ctas));

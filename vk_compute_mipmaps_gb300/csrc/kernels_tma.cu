@@ -40,6 +40,9 @@
 // count == gridDim.x - 1 after a release/acquire fence pair) runs those
 // dispatches itself, reading the freshly written level with L2-coherent
 // loads.  No thread waits on another CTA, so there is no spin on a flag.
+// Every CTA arrives, also one whose bounded wait gave up (it then marks its
+// arrival as failed and the last CTA skips the tail), so the counter is back
+// at zero when the kernel ends, whatever happened.
 #include <cuda.h>
 
 #include <atomic>
@@ -69,6 +72,9 @@ constexpr uint32_t kMaxFused = 4;
 constexpr uint32_t kSuspendHintNs = 20000;
 constexpr uint32_t kWaitLimitNs = 1000000000u;
 constexpr uint32_t kWaitPolls = 1u << 22;
+// Tail counter arrivals: the low 16 bits count CTAs (grids are at most one
+// CTA per SM), a CTA whose wait gave up adds this as well.
+constexpr uint32_t kFailedArrival = 1u << 16;
 
 // Byte offsets inside the dynamic shared memory block.
 constexpr uint32_t kLutDecodeOff = 0;                          // 256 rows x 256 B
@@ -78,7 +84,8 @@ constexpr uint32_t kXchgOff = kStageOff + kGroups * kStages * kTileBytes;  // [g
 constexpr uint32_t kBarOff = kXchgOff + kGroups * kXchgRing * 16 * 16;     // mbarriers, per group:
 // full[stage], empty[stage], xfull[ring], xempty[ring]
 constexpr uint32_t kBarsPerGroup = 2 * kStages + 2 * kXchgRing;
-constexpr uint32_t kSmemBytes = kBarOff + kGroups * kBarsPerGroup * 8;
+constexpr uint32_t kIssuedOff = kBarOff + kGroups * kBarsPerGroup * 8;  // [group][stage] TMA loads issued
+constexpr uint32_t kSmemBytes = kIssuedOff + kGroups * kStages * 4;
 static_assert(kStageOff % 128 == 0, "TMA destinations need 128-byte alignment");
 static_assert(kSmemBytes <= 232448, "exceeds the 227 KiB of shared memory per CTA");
 constexpr uint32_t kDebugSmemBytes = kLutThrOff + kThrRows * 128;
@@ -98,6 +105,9 @@ struct TmaParams {
   uint32_t stageCount;
   uint32_t* counter;    // last-CTA-done counter (self-resetting)
   uint32_t* errorFlag;  // set to 1 if a bounded wait gave up
+  // Test support: this CTA gives up at once, as if its first wait had run out
+  // (no CTA when out of range).
+  uint32_t failCta;
 };
 
 __device__ __forceinline__ Lut makeLut(uint32_t lane) {
@@ -278,6 +288,7 @@ struct GroupCtx {
   uint32_t xfull0;
   uint32_t xempty0;
   float4* xchg;           // this group's exchange ring
+  uint32_t* issued;       // TMA loads issued per stage (producer lane 0 only)
 };
 
 __device__ __forceinline__ GroupCtx groupCtx(uint32_t g) {
@@ -290,6 +301,7 @@ __device__ __forceinline__ GroupCtx groupCtx(uint32_t g) {
   G.xfull0 = G.empty0 + 8 * kStages;
   G.xempty0 = G.xfull0 + 8 * kXchgRing;
   G.xchg = reinterpret_cast<float4*>(smem + kXchgOff) + g * kXchgRing * 16;
+  G.issued = reinterpret_cast<uint32_t*>(smem + kIssuedOff) + g * kStages;
   return G;
 }
 
@@ -364,8 +376,10 @@ __device__ __forceinline__ bool producerLoop(const FusedStage& st, const CUtenso
     const uint32_t s = iter & 1, parity = (iter >> 1) & 1;
     if (ahead.ry < st.regionsY) {
       if (!mbarWait(G.empty0 + 8 * s, parity)) return false;
-      if (lane == 0)
+      if (lane == 0) {
         tmaLoadRegion(G.stage0 + s * kTileBytes, map, ahead.rx * kTile, ahead.ry * kTile, G.full0 + 8 * s);
+        ++G.issued[s];
+      }
     }
     if (N >= 5) {
       if (!mbarWait(G.xfull0 + 8 * s, parity)) return false;
@@ -476,6 +490,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  if (tid < kGroups * kStages) reinterpret_cast<uint32_t*>(smem + kIssuedOff)[tid] = 0;
   __syncthreads();
   const Lut L = makeLut(lane);
   // Programmatic dependent launch: everything above (tables, barriers) may
@@ -494,33 +509,42 @@ __global__ void __launch_bounds__(kThreads, 1)
     const GroupCtx G = groupCtx(g);
     for (uint32_t s = 0; s < kStages; ++s) {
       const uint32_t r = g * gridDim.x + blockIdx.x + s * groupsTotal;
-      if (r < regions)
+      if (r < regions) {
         tmaLoadRegion(G.stage0 + s * kTileBytes, &tmap, (r % s0.regionsX) * kTile, (r / s0.regionsX) * kTile,
                       G.full0 + 8 * s);
+        ++G.issued[s];
+      }
     }
   }
   __syncwarp();
-  const bool ok = mainLoopN<SF>(s0, &tmap, warp, groupsTotal, lane, L);
-  if (!ok && lane == 0) {
-    // A bounded wait gave up: record it and give the loads that may still be
-    // in flight one more bounded wait before the CTA may exit.
+  const bool ok = blockIdx.x != p.failCta && mainLoopN<SF>(s0, &tmap, warp, groupsTotal, lane, L);
+  const bool failed = __syncthreads_or(!ok);
+  if (failed && tid == 0) {
+    // A bounded wait gave up: record it, and wait (bounded) for the last load
+    // issued into each buffer, which may still be in flight, before the CTA
+    // may exit.  Load n of a buffer completes phase n - 1 of its mbarrier.
     atomicExch(p.errorFlag, 1u);
-    for (uint32_t g = 0; g < kGroups; ++g)
-      for (uint32_t s = 0; s < kStages; ++s) {
-        mbarWait(groupCtx(g).full0 + 8 * s, 0);
-        mbarWait(groupCtx(g).full0 + 8 * s, 1);
-      }
+    for (uint32_t g = 0; g < kGroups; ++g) {
+      const GroupCtx G = groupCtx(g);
+      for (uint32_t s = 0; s < kStages; ++s)
+        if (G.issued[s]) mbarWait(G.full0 + 8 * s, (G.issued[s] - 1) & 1);
+    }
   }
-  if (__syncthreads_or(!ok) || p.stageCount < 2) return;
+  if (p.stageCount < 2) return;
 
   // ---- last CTA runs the trailing dispatches ----
+  // Every CTA arrives, a failed one with kFailedArrival added, so the counter
+  // always returns to zero (no later launch sees a partial count); the tail
+  // is skipped when any CTA failed, since its input level is incomplete.
   uint32_t last = 0;
   if (tid == 0) {
     __threadfence();
-    last = atomicAdd(p.counter, 1u) == gridDim.x - 1;
-    if (last) {
+    const uint32_t inc = failed ? kFailedArrival + 1 : 1u;
+    const uint32_t total = atomicAdd(p.counter, inc) + inc;
+    if ((total & (kFailedArrival - 1)) == gridDim.x) {
       *p.counter = 0;
       __threadfence();
+      last = total < kFailedArrival;
     }
   }
   if (!__syncthreads_or(last) || warp >= kProducerWarp0) return;
@@ -701,11 +725,12 @@ bool tmaTailCompatible(const DispatchParams& prev, const DispatchParams& next) {
 uint32_t tmaMaxFused() { return kMaxFused; }
 
 cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, uint32_t tailCount,
-                          cudaStream_t stream, const Scratch& scratch, uint32_t* launches) {
+                          cudaStream_t stream, const Scratch& scratch, uint32_t* launches, uint32_t debugFailCta) {
   DeviceInfo* info = nullptr;
   cudaError_t e = deviceInfo(&info);
   if (e != cudaSuccess) return e;
-  if (tailCount + 1 > kMaxFused || (tailCount && scratch.counterCount < 2)) return cudaErrorInvalidValue;
+  if (tailCount + 1 > kMaxFused || (tailCount && scratch.counterCount < kTmaScratchWords))
+    return cudaErrorInvalidValue;
   for (uint32_t i = 0; i < tailCount; ++i)
     if (tail[i].sharedFmt != p.sharedFmt) return cudaErrorInvalidValue;  // one shared format per launch
   TmaParams tp{};
@@ -713,7 +738,8 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
   for (uint32_t i = 0; i < tailCount; ++i) fillStage(tail[i], &tp.st[i + 1]);
   tp.stageCount = 1 + tailCount;
   tp.counter = scratch.counters;
-  tp.errorFlag = scratch.counters ? scratch.counters + 1 : nullptr;
+  tp.errorFlag = scratch.counters ? scratch.error() : nullptr;
+  tp.failCta = tp.errorFlag ? debugFailCta : ~0u;
 
   CUtensorMap map;
   const cuuint64_t dims[2] = {p.lv[0].w, p.lv[0].h};
@@ -743,29 +769,56 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
   return cudaGetLastError();
 }
 
-// Device scratch for nvproPyramidGenerateNoAlloc: the last-CTA counter and
-// the wait-error flag of each TMA launch of a chain, two words per launch.
-// It is a file-scope __device__ array, so every GPU that loads the library
-// holds these 256 bytes until the process exits, and no call allocates.
+// Device scratch for nvproPyramidGenerateNoAlloc: the shared error flag and
+// the per-launch counters of a chain (see kStaticScratchWords).  It is a
+// file-scope __device__ array, so every GPU that loads the library holds these
+// 1 KiB until the process exits, and no call allocates.
 static __device__ __align__(256) uint32_t g_staticScratch[kStaticScratchWords];
 
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+
+CtxGetCurrentFn ctxGetCurrent() {
+  static CtxGetCurrentFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return CtxGetCurrentFn(nullptr);
+    return reinterpret_cast<CtxGetCurrentFn>(p);
+  }();
+  return fn;
+}
+
 cudaError_t staticScratch(uint32_t** ptr) {
-  static uint32_t* addrs[64] = {};
+  struct Entry {
+    CUcontext ctx;
+    uint32_t* addr;
+  };
+  static Entry entries[64] = {};
   static std::mutex mu;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  CtxGetCurrentFn getCtx = ctxGetCurrent();
+  CUcontext ctx = nullptr;
+  if (getCtx && getCtx(&ctx) != CUDA_SUCCESS) ctx = nullptr;
   std::lock_guard<std::mutex> lock(mu);
-  if (!addrs[dev]) {
+  Entry& d = entries[dev];
+  // A context that is not the one of the cached address (none yet, or the
+  // device was reset and its context made anew, which may load the module at
+  // another address) gets a fresh look-up.
+  if (!d.addr || !ctx || ctx != d.ctx) {
     // In host code the array's name is a host-side stand-in; its device
-    // address comes from the runtime, once per device, with that device current.
+    // address comes from the runtime, with the device current.
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_staticScratch);
     if (e != cudaSuccess) return e;
-    addrs[dev] = static_cast<uint32_t*>(p);
+    if (getCtx && getCtx(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+    d.addr = static_cast<uint32_t*>(p);
+    d.ctx = ctx;
   }
-  *ptr = addrs[dev];
+  *ptr = d.addr;
   return cudaSuccess;
 }
 

@@ -43,3 +43,19 @@ def smooth_field(w: int, h: int, seed: int, opaque: bool = False) -> np.ndarray:
     r = np.hypot(x - w / 2, y - h / 2) / max(np.hypot(w / 2, h / 2), 1)
     img[..., 3] = 255 if opaque else 255 * (1 - r)
     return np.clip(np.rint(img), 0, 255).astype(np.uint8)
+
+
+def shard_by_image(sizes, rank: int, world: int) -> list[int]:
+    """Indices of the images rank `rank` of `world` generates when a batch is
+    split by image (no exchange between ranks: every image is independent).
+    Largest chains first, each to the rank with the fewest bytes so far (ties
+    to the lowest rank), so every rank gets about the same traffic; the same
+    on every rank, so the shares are disjoint and cover the batch."""
+    load = [0] * world
+    owner = [0] * len(sizes)
+    order = sorted(range(len(sizes)), key=lambda i: (-chain_bytes(*sizes[i]), i))
+    for i in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[i] = r
+        load[r] += chain_bytes(*sizes[i])
+    return [i for i in range(len(sizes)) if owner[i] == rank]
