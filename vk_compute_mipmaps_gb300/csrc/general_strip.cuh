@@ -28,9 +28,8 @@
 namespace nvpyr {
 namespace {
 
-constexpr uint32_t kCols2 = 15;     // level-(L+2) columns per strip (two levels)
-constexpr uint32_t kCols1 = 31;     // level-(L+1) columns per strip (one level)
-constexpr uint32_t kGroupRows = 4;  // level-(L+1) rows whose level-L rows load together
+constexpr uint32_t kCols2 = 31;     // level-(L+2) columns per strip (two levels)
+constexpr uint32_t kCols1 = 63;     // level-(L+1) columns per strip (one level)
 constexpr uint32_t kWaitLimit = 1u << 22;  // grid barrier polls (with backoff: about a second)
 constexpr uint32_t kTightPolls = 512;      // polls before the backoff starts
 
@@ -115,175 +114,193 @@ __device__ __forceinline__ float4 decodeAligned(uint32_t w, const Lut& L) {
 
 // One strip of a one- or two-level dispatch.  TX0 / TY0: three-tap kernel
 // from level L along x / y (else two taps); TX1 / TY1: the same from level
-// L+1 (two levels only).  The flags are uniform across the grid, so their
-// branches never diverge; one code path for all of them keeps the chain
-// kernel free of calls.  SF: the pipeline's shared format, applied to the
-// level-(L+1) values that level L+2 is reduced from (sharedLevel_,
-// nvpro_pyramid.glsl:664,717).
-// strip<SF, V>: V fixes the stage's variant at compile time, or kRuntimeVariant
-// reads it once from the stage (measured: a single read of the variant instead
-// of one per flag took 4095^2 from 75.8 to 73.7 us and the 256-image batch
-// from 1454 to 1375 us; a second, variant-15 copy in the chain kernel spilled).
-constexpr uint32_t kRuntimeVariant = 255;
+// L+1 (two levels only).  The flags are read once from the stage's variant;
+// they are uniform across the grid, so their branches never diverge.  SF: the
+// pipeline's shared format, applied to the level-(L+1) values that level L+2
+// is reduced from (sharedLevel_, nvpro_pyramid.glsl:664,717).
+//
+// Lane l owns level-(L+1) columns xa = x0 + 2l and xb = xa + 1 and level-(L+2)
+// column X0 + l, and loads level-L columns 2xa .. 2xa + 3; the third tap
+// 2xb + 2 of xb is lane l+1's first column, and the third level-(L+1) column
+// 2X + 2 of X is lane l+1's xa (shfl.down 1 of the vertically reduced values).
+// A strip is 31 level-(L+2) columns (62 level-(L+1) columns stored; lane 31
+// only feeds lane 30, and stores xa in the last strip) or 63 level-(L+1)
+// columns for one-level dispatches.  Each step reduces two level-(L+1) rows
+// (rA, rB = rA + 1) from four new level-L rows and, for two levels, one
+// level-(L+2) row; the next step's four rows load while this one reduces.
+// Operation order (reduceStoreSample_, nvpro_pyramid.glsl:575-656): per
+// column vertical first, then horizontal, every multiply and add rounded
+// separately, as in the oracle.
+__device__ __forceinline__ float4 colReduce(bool three, const Weights3& w, float4 a, float4 b, float4 c) {
+  return three ? reduce3p(w, a, b, c) : reduce2p(a, b);
+}
 
-// ROWS: level-(L+1) rows whose level-L rows load together (the prefetch
-// depth); 4 in the chain kernel, 2 in the batch kernel, whose units are
-// shorter (measured: 2 rows took the 256-image batch from 1375 to 1313 us
-// but the 4095^2 chain from 74 to 78 us).
-template <uint32_t SF, uint32_t V = kRuntimeVariant, uint32_t ROWS = kGroupRows>
+template <uint32_t SF>
 __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t band, uint32_t lane, const Lut& lut) {
-  const uint32_t variant = V == kRuntimeVariant ? st.variant : V;
-  const uint32_t LEVELS = variant >= 16 ? 1u : 2u;
-  const bool TX0 = LEVELS == 2 ? (variant & 8) != 0 : (variant & 2) != 0;
-  const bool TY0 = LEVELS == 2 ? (variant & 4) != 0 : (variant & 1) != 0;
-  const bool TX1 = LEVELS == 2 && (variant & 2) != 0;
-  const bool TY1 = LEVELS == 2 && (variant & 1) != 0;
+  const uint32_t variant = st.variant;
+  const bool two = variant < 16;
+  const bool TX0 = two ? (variant & 8) != 0 : (variant & 2) != 0;
+  const bool TY0 = two ? (variant & 4) != 0 : (variant & 1) != 0;
+  const bool TX1 = two && (variant & 2) != 0;
+  const bool TY1 = two && (variant & 1) != 0;
   // Every field in a register before the first store: stores through
   // generic pointers would otherwise force reloads of a stage held in memory.
   const Lut L = lut;
-  struct {
-    const uint8_t* src;
-    uint64_t srcPitch;
-    uint32_t w0, h0;
-    uint8_t* dst1;
-    uint64_t pitch1;
-    uint32_t w1, h1;
-    uint8_t* dst2;
-    uint64_t pitch2;
-    uint32_t w2, h2, band;
-  } const p = {st.src, st.srcPitch, st.w0, st.h0, st.dst1, st.pitch1, st.w1, st.h1, st.dst2, st.pitch2, st.w2, st.h2,
-               st.band};
-  const uint32_t cols = LEVELS == 2 ? 2 * kCols2 : kCols1;  // level-(L+1) columns owned by a strip
-  const uint32_t x0 = tile * cols;
-  const uint32_t x = x0 + lane;
-  // level-L columns of this lane, clamped into the level for lanes past its edge
-  const uint8_t* colA = p.src + uint64_t(min(2 * x, p.w0 - 1)) * 4;
-  const uint8_t* colB = p.src + uint64_t(min(2 * x + 1, p.w0 - 1)) * 4;
-  const Axis3 ax1 = axis3(p.w1), ay1 = axis3(p.h1);
-  const Weights3 wx = weightsAt(ax1, min(x, p.w1 - 1));
+  const uint8_t* const src = st.src;
+  const uint64_t pitch = st.srcPitch;
+  const uint32_t w0 = st.w0;
+  uint8_t* const dst1 = st.dst1;
+  const uint64_t pitch1 = st.pitch1;
+  const uint32_t w1 = st.w1, h1 = st.h1;
+  uint8_t* const dst2 = st.dst2;
+  const uint64_t pitch2 = st.pitch2;
+  const uint32_t w2 = st.w2, h2 = st.h2, bandRows = st.band;
 
-  // rows [yb, ye) of level L+1, of which [yb, yStoreEnd) are this strip's
+  const uint32_t x0 = tile * (two ? 2 * kCols2 : kCols1);
+  const uint32_t xa = x0 + 2 * lane, xb = xa + 1;
+  const bool lastTile = (tile + 1) * (two ? kCols2 : kCols1) >= (two ? w2 : w1);
+  // lane 31's xa belongs to a one-level strip (63 columns); in a two-level one
+  // it is the next strip's first column, except in the last strip
+  const bool storeA = xa < w1 && (lane < 31 || !two || lastTile);
+  const bool storeB = xb < w1 && lane < 31;
+  const uint32_t X = x0 / 2 + lane;  // this lane's level-(L+2) column
+  const bool storeX = two && lane < 31 && X < w2;
+  // level-L columns 2xa .. 2xa + 3, clamped into the level (clamped ones feed
+  // no stored texel)
+  const uint32_t ca = min(2 * xa, w0 - 1);
+  const uint8_t* const colA = src + uint64_t(ca) * 4;
+  const uint32_t d1 = (min(2 * xa + 1, w0 - 1) - ca) * 4, d2 = (min(2 * xa + 2, w0 - 1) - ca) * 4,
+                 d3 = (min(2 * xa + 3, w0 - 1) - ca) * 4;
+  const Axis3 ax1 = axis3(w1), ay1 = axis3(h1), ax2 = axis3(w2), ay2 = axis3(h2);
+  const Weights3 wxa = weightsAt(ax1, min(xa, w1 - 1)), wxb = weightsAt(ax1, min(xb, w1 - 1));
+  const Weights3 wX = weightsAt(ax2, min(X, w2 - 1));
+
+  // level-(L+1) rows [yb, ye) of this band, of which [yb, yStoreEnd) are stored here
   uint32_t yb, ye, yStoreEnd;
-  bool store1x;
-  if (LEVELS == 2) {
-    const uint32_t Yb = band * p.band, Ye = min(Yb + p.band, p.h2);
+  if (two) {
+    const uint32_t Yb = band * bandRows, Ye = min(Yb + bandRows, h2);
     yb = 2 * Yb;
     ye = 2 * Ye + (TY1 ? 1 : 0);
-    yStoreEnd = Ye == p.h2 ? p.h1 : 2 * Ye;
-    const bool lastTile = (tile + 1) * kCols2 >= p.w2;
-    store1x = x < p.w1 && (lane < cols || lastTile);
+    yStoreEnd = Ye == h2 ? h1 : 2 * Ye;
   } else {
-    yb = band * p.band;
-    ye = min(yb + p.band, p.h1);
+    yb = band * bandRows;
+    ye = min(yb + bandRows, h1);
     yStoreEnd = ye;
-    store1x = x < p.w1 && lane < cols;
   }
-  const uint32_t X = x0 / 2 + (lane >> 1);  // level-(L+2) column of an even lane
-  const bool store2x = LEVELS == 2 && (lane & 1) == 0 && lane < 2 * kCols2 && X < p.w2;
-  const Axis3 ax2 = axis3(p.w2), ay2 = axis3(p.h2);
-  const Weights3 wX = weightsAt(ax2, min(X, p.w2 - 1));
 
-  // Level-L rows: lane texels at colA / colA + dB of row r.  Rows are read
-  // only while their level-(L+1) row is inside the band, so no row index
-  // leaves the level (for y < ye: 2y + 2 <= h0 - 1 with three taps, 2y + 1
-  // <= h0 - 1 with two).
-  const uint32_t dB = uint32_t(colB - colA);  // 4, or 0 where column 2x+1 is clamped
-  const uint64_t pitch = p.srcPitch;
-  auto ldGroup = [&](uint32_t yg, uint32_t (&raw)[ROWS][4]) {
-    const uint8_t* row = colA + uint64_t(TY0 ? 2 * yg + 1 : 2 * yg) * pitch;
+  // four level-L rows from `row0`, the lane's four columns each; rows at or
+  // beyond `rowEnd` are not read
+  auto ldRows = [&](uint32_t row0, uint32_t rowEnd, uint32_t (&raw)[4][4]) {
+    const uint8_t* p = colA + uint64_t(row0) * pitch;
 #pragma unroll
-    for (uint32_t j = 0; j < ROWS; ++j) {
-      if (yg + j < ye) {
-        raw[j][0] = ldTexel(row);
-        raw[j][1] = ldTexel(row + dB);
-        raw[j][2] = ldTexel(row + pitch);
-        raw[j][3] = ldTexel(row + pitch + dB);
+    for (uint32_t j = 0; j < 4; ++j) {
+      if (row0 + j < rowEnd) {
+        raw[j][0] = ldTexel(p);
+        raw[j][1] = ldTexel(p + d1);
+        raw[j][2] = ldTexel(p + d2);
+        raw[j][3] = ldTexel(p + d3);
       }
-      row += 2 * pitch;
+      p += pitch;
+    }
+  };
+  auto decodeRow = [&](const uint32_t (&r)[4], float4 (&d)[4]) {
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) d[k] = decodeAligned(r[k], L);
+  };
+
+  // Level-(L+1) row y from level-L rows (carry = row 2y when TY0, r1, r2):
+  // vertical per column, then the two horizontal reductions; stores them and
+  // returns their FP32 values (after the shared format) in a / b.
+  float4 carry[4];  // TY0: decoded level-L row 2y of the next level-(L+1) row
+  auto level1Row = [&](uint32_t y, const uint32_t (&r1)[4], const uint32_t (&r2)[4], float4& a, float4& b) {
+    float4 d1v[4], d2v[4], v[4];
+    decodeRow(r1, d1v);
+    decodeRow(r2, d2v);
+    if (TY0) {
+      const Weights3 wy = weightsAt(ay1, y);
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) v[k] = reduce3p(wy, carry[k], d1v[k], d2v[k]);
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) carry[k] = d2v[k];
+    } else {
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) v[k] = reduce2p(d1v[k], d2v[k]);
+    }
+    const float4 v4 = shflDown(v[0], 1);
+    a = colReduce(TX0, wxa, v[0], v[1], v[2]);
+    b = TX0 ? reduce3p(wxb, v[2], v[3], v4) : reduce2p(v[2], v[3]);
+    const uint32_t ea = encodeTexel(a, L), eb = encodeTexel(b, L);
+    const bool rowOk = y < yStoreEnd;
+    uint8_t* const out = dst1 + uint64_t(y) * pitch1 + uint64_t(xa) * 4;
+    storeIf(storeA && rowOk, out, ea);
+    storeIf(storeB && rowOk, out + 4, eb);
+    if (SF == kSharedSrgb) {
+      a = decodeAligned(ea, L);
+      b = decodeAligned(eb, L);
+    }
+    if (SF == kSharedF16) {
+      a = f16RoundTrip(a);
+      b = f16RoundTrip(b);
     }
   };
 
-  float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;  // three taps: level-L row 2y
-  if (TY0) {
-    const uint8_t* row = colA + uint64_t(2 * yb) * pitch;
-    pa = decodeAligned(ldTexel(row), L);
-    pb = decodeAligned(ldTexel(row + dB), L);
+  // first level-(L+1) row of the steps: rA = yb (+1 when TY1: row yb comes first, alone)
+  const uint32_t l0End = 2 * ye + (TY0 ? 1 : 0);  // level-L rows this band reads: [.., l0End)
+  float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;  // TY1: level-(L+1) row 2Y of the next level-(L+2) row
+  uint32_t y = yb;
+  if (TY0) {  // level-L row 2yb
+    uint32_t r0[4];
+    const uint8_t* p = colA + uint64_t(2 * yb) * pitch;
+    r0[0] = ldTexel(p);
+    r0[1] = ldTexel(p + d1);
+    r0[2] = ldTexel(p + d2);
+    r0[3] = ldTexel(p + d3);
+    decodeRow(r0, carry);
   }
-  float4 h0v = make_float4(0.f, 0.f, 0.f, 0.f), h1v = h0v;  // level-(L+1) rows 2Y, 2Y+1
-
-  auto process = [&](uint32_t yg, const uint32_t (&raw)[ROWS][4]) {
-#pragma unroll
-    for (uint32_t j = 0; j < ROWS; ++j) {
-      const uint32_t y = yg + j;
-      if (y >= ye) break;
-      const float4 r1a = decodeAligned(raw[j][0], L), r1b = decodeAligned(raw[j][1], L);
-      const float4 r2a = decodeAligned(raw[j][2], L), r2b = decodeAligned(raw[j][3], L);
-      float4 va, vb;
-      if (TY0) {
-        const Weights3 wy = weightsAt(ay1, y);
-        va = reduce3p(wy, pa, r1a, r2a);
-        vb = reduce3p(wy, pb, r1b, r2b);
-        pa = r2a;
-        pb = r2b;
+  if (TY1) {  // level-(L+1) row yb alone: the top row of the first level-(L+2) row
+    uint32_t r[4][4];
+    ldRows(2 * yb + (TY0 ? 1 : 0), 2 * yb + (TY0 ? 3 : 2), r);
+    level1Row(y, r[0], r[1], pa, pb);
+    ++y;
+  }
+  // steps of two level-(L+1) rows (y, y + 1); level-L rows from 2y (+1 with TY0)
+  uint32_t bufA[4][4], bufB[4][4];
+  const uint32_t off = TY0 ? 1 : 0;
+  if (y < ye) ldRows(2 * y + off, l0End, bufA);
+  auto step = [&](uint32_t yy, const uint32_t (&r)[4][4]) {
+    float4 aA, bA, aB = make_float4(0.f, 0.f, 0.f, 0.f), bB = aB;
+    level1Row(yy, r[0], r[1], aA, bA);
+    if (yy + 1 < ye) level1Row(yy + 1, r[2], r[3], aB, bB);
+    if (two) {
+      // level-(L+2) row Y from level-(L+1) rows 2Y (pa, pb), 2Y+1, 2Y+2 (TY1) or 2Y, 2Y+1
+      float4 ua, ub;
+      uint32_t Y;
+      if (TY1) {
+        Y = (yy - 1) >> 1;
+        const Weights3 wY = weightsAt(ay2, Y);
+        ua = reduce3p(wY, pa, aA, aB);
+        ub = reduce3p(wY, pb, bA, bB);
+        pa = aB;
+        pb = bB;
       } else {
-        va = reduce2p(r1a, r2a);
-        vb = reduce2p(r1b, r2b);
+        Y = yy >> 1;
+        ua = reduce2p(aA, aB);
+        ub = reduce2p(bA, bB);
       }
-      float4 l1;
-      if (TX0)
-        l1 = reduce3p(wx, va, vb, shflDown(va, 1));
-      else
-        l1 = reduce2p(va, vb);
-      const uint32_t code1 = encodeTexel(l1, L);
-      storeIf(store1x && y < yStoreEnd, p.dst1 + uint64_t(y) * p.pitch1 + uint64_t(x) * 4, code1);
-      if (LEVELS == 2) {
-        if (SF == kSharedSrgb) l1 = decodeAligned(code1, L);
-        if (SF == kSharedF16) l1 = f16RoundTrip(l1);
-        const uint32_t jj = y - yb;
-        bool emit = false;
-        uint32_t Y = 0;
-        float4 v2 = l1;
-        if (TY1) {
-          if (jj == 0) {
-            h0v = l1;
-          } else if (jj & 1) {
-            h1v = l1;
-          } else {
-            Y = (y - 2) >> 1;
-            v2 = reduce3p(weightsAt(ay2, Y), h0v, h1v, l1);
-            h0v = l1;
-            emit = true;
-          }
-        } else {
-          if ((jj & 1) == 0) {
-            h0v = l1;
-          } else {
-            Y = (y - 1) >> 1;
-            v2 = reduce2p(h0v, l1);
-            emit = true;
-          }
-        }
-        if (emit) {
-          const float4 n1 = shflDown(v2, 1);
-          const float4 o = TX1 ? reduce3p(wX, v2, n1, shflDown(v2, 2)) : reduce2p(v2, n1);
-          storeIf(store2x, p.dst2 + uint64_t(Y) * p.pitch2 + uint64_t(X) * 4, encodeTexel(o, L));
-        }
-      }
+      const float4 uc = shflDown(ua, 1);
+      const float4 o = TX1 ? reduce3p(wX, ua, ub, uc) : reduce2p(ua, ub);
+      storeIf(storeX, dst2 + uint64_t(Y) * pitch2 + uint64_t(X) * 4, encodeTexel(o, L));
     }
   };
-
-  // two row buffers in turn: the next group's rows load while this one reduces
-  uint32_t bufA[ROWS][4], bufB[ROWS][4];
-  ldGroup(yb, bufA);
-  for (uint32_t yg = yb;;) {
-    if (yg + ROWS < ye) ldGroup(yg + ROWS, bufB);
-    process(yg, bufA);
-    yg += ROWS;
-    if (yg >= ye) break;
-    if (yg + ROWS < ye) ldGroup(yg + ROWS, bufA);
-    process(yg, bufB);
-    yg += ROWS;
-    if (yg >= ye) break;
+  for (;;) {
+    if (y >= ye) break;
+    if (y + 2 < ye) ldRows(2 * (y + 2) + off, l0End, bufB);
+    step(y, bufA);
+    y += 2;
+    if (y >= ye) break;
+    if (y + 2 < ye) ldRows(2 * (y + 2) + off, l0End, bufA);
+    step(y, bufB);
+    y += 2;
   }
 }
 

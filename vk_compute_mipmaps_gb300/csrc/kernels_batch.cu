@@ -31,7 +31,7 @@
 namespace nvpyr {
 namespace {
 
-constexpr uint32_t kWarps = 16;
+constexpr uint32_t kWarps = 12;
 constexpr uint32_t kThreads = 32 * kWarps;
 constexpr uint32_t kRegion = 64;  // fast units: 64x64 texels of level L
 constexpr uint32_t kTopBytes = kMaxDispatchLevels * 32 * 16;  // per warp: fast-region rows kept per level
@@ -225,7 +225,7 @@ __device__ __noinline__ void tinyGeneral(const TinyJob& tj, uint32_t lane, const
 // Out of line, each unit kind gets its own register allocation; the call
 // costs a few register saves per unit.
 __device__ __noinline__ void stripUnit(const Stage& st, uint32_t local, uint32_t lane, const Lut& L) {
-  strip<kSharedFp32, kRuntimeVariant, 2>(st, local % st.tilesX, local / st.tilesX, lane, L);
+  strip<kSharedFp32>(st, local % st.tilesX, local / st.tilesX, lane, L);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) batchKernel(const __grid_constant__ BatchParams p) {

@@ -18,7 +18,7 @@
 namespace nvpyr {
 namespace {
 
-constexpr uint32_t kWarps = 16;
+constexpr uint32_t kWarps = 12;
 constexpr uint32_t kThreads = 32 * kWarps;
 constexpr uint32_t kCtasPerSm = 1;
 constexpr uint32_t kMaxStages = 16;
@@ -39,11 +39,10 @@ __device__ __forceinline__ bool gridBarrier(const ChainParams& p, uint32_t& gen,
   return gridBarrierWait(p.barrierCount, p.barrierGen, p.errorFlag, gen, okFlag);
 }
 
-template <uint32_t SF, uint32_t ROWS>
+template <uint32_t SF>
 __device__ __forceinline__ void runStage(const Stage& st, uint32_t lane, uint32_t warpId, uint32_t warps, const Lut& L) {
   const uint32_t units = st.tilesX * st.bands;
-  for (uint32_t u = warpId; u < units; u += warps)
-    strip<SF, kRuntimeVariant, ROWS>(st, u % st.tilesX, u / st.tilesX, lane, L);
+  for (uint32_t u = warpId; u < units; u += warps) strip<SF>(st, u % st.tilesX, u / st.tilesX, lane, L);
 }
 
 // Every CTA of a multi-stage launch arrives here once on its way out.  The
@@ -62,9 +61,8 @@ __device__ __forceinline__ void exitArrive(const ChainParams& p) {
   }
 }
 
-// SF: the general pipeline's shared format (one per launch); ROWS: the strip's
-// prefetch depth (2 for runs that start on a small level, whose bands are short).
-template <uint32_t SF, uint32_t ROWS>
+// SF: the general pipeline's shared format (one per launch).
+template <uint32_t SF>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const __grid_constant__ ChainParams p) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint32_t okFlag;
@@ -78,7 +76,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
 #pragma unroll 1
   for (uint32_t s = 0; s < p.stageCount; ++s) {
     const bool alone = s >= p.tailFrom;  // a small stage: this CTA alone
-    runStage<SF, ROWS>(p.st[s], lane, alone ? localWarp : warpId, alone ? kWarps : warps, L);
+    runStage<SF>(p.st[s], lane, alone ? localWarp : warpId, alone ? kWarps : warps, L);
     if (s + 1 == p.stageCount) break;
     if (s + 1 < p.tailFrom) {
       if (!gridBarrier(p, gen, &okFlag)) break;
@@ -110,19 +108,10 @@ struct DeviceState {
   int ctasPerSm = 0;
 };
 
-template <uint32_t ROWS>
-const void* chainKernelRows(uint32_t sharedFmt) {
-  return sharedFmt == kSharedSrgb  ? reinterpret_cast<const void*>(generalChainKernel<kSharedSrgb, ROWS>)
-         : sharedFmt == kSharedF16 ? reinterpret_cast<const void*>(generalChainKernel<kSharedF16, ROWS>)
-                                   : reinterpret_cast<const void*>(generalChainKernel<kSharedFp32, ROWS>);
-}
-
-// The launch's kernel.  Runs whose first input level is under kShortLevelRows
-// rows use the 2-row prefetch (measured: 1920x1080, whose general run starts
-// on 240x135, 34.8 -> 31.7 us; the 4095^2 chain is faster with 4 rows).
-constexpr uint32_t kShortLevelRows = 512;
-const void* chainKernel(uint32_t sharedFmt, bool shortLevels) {
-  return shortLevels ? chainKernelRows<2>(sharedFmt) : chainKernelRows<kGroupRows>(sharedFmt);
+const void* chainKernel(uint32_t sharedFmt) {
+  return sharedFmt == kSharedSrgb  ? reinterpret_cast<const void*>(generalChainKernel<kSharedSrgb>)
+         : sharedFmt == kSharedF16 ? reinterpret_cast<const void*>(generalChainKernel<kSharedF16>)
+                                   : reinterpret_cast<const void*>(generalChainKernel<kSharedFp32>);
 }
 
 cudaError_t deviceState(int* sms, int* ctasPerSm) {
@@ -139,13 +128,11 @@ cudaError_t deviceState(int* sms, int* ctasPerSm) {
     e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (e != cudaSuccess) return e;
     if (!coop) return cudaErrorNotSupported;
-    for (const bool shortLevels : {false, true})
-      for (const uint32_t fmt : {kSharedFp32, kSharedSrgb, kSharedF16}) {
-        e = cudaFuncSetAttribute(chainKernel(fmt, shortLevels), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(kSmemBytes));
-        if (e != cudaSuccess) return e;
-      }
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.ctasPerSm, generalChainKernel<kSharedFp32, kGroupRows>,
+    for (const uint32_t fmt : {kSharedFp32, kSharedSrgb, kSharedF16}) {
+      e = cudaFuncSetAttribute(chainKernel(fmt), cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
+      if (e != cudaSuccess) return e;
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.ctasPerSm, generalChainKernel<kSharedFp32>,
                                                       kThreads, kSmemBytes);
     if (e != cudaSuccess) return e;
     if (d.ctasPerSm < 1) return cudaErrorInvalidConfiguration;
@@ -223,7 +210,7 @@ cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStre
   uint32_t grid = count > 1 ? ctas : uint32_t(std::min<uint64_t>((maxUnits + kWarps - 1) / kWarps, ctas));
   if (cp.tailFrom == 0) grid = 1;
   void* args[] = {&cp};
-  e = cudaLaunchCooperativeKernel(chainKernel(p[0].sharedFmt, p[0].lv[0].h < kShortLevelRows), dim3(grid),
+  e = cudaLaunchCooperativeKernel(chainKernel(p[0].sharedFmt), dim3(grid),
                                   dim3(kThreads), args, kSmemBytes, stream);
   if (e != cudaSuccess) return e;
   ++*launches;
