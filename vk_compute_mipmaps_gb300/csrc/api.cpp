@@ -148,6 +148,85 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
   return NVPRO_PYRAMID_SUCCESS;
 }
 
+// How recorded dispatches become kernel launches.
+enum LaunchKind : uint32_t {
+  kLaunchTma = 0,      // the TMA fast kernel: dispatch `first`, then `small` small dispatches in its tail
+  kLaunchGeneral = 1,  // the general chain: `big` strip stages from `first`, then `small` small dispatches
+  kLaunchSmall = 2,    // one CTA: `small` small dispatches from `first`
+  kLaunchPortable = 3  // the portable kernels: dispatch `first`
+};
+struct LaunchPlan {
+  uint32_t kind, first, big, small;
+  // scratch words the launch needs (the counters of launches of several parts)
+  uint32_t words() const {
+    if (kind == kLaunchTma) return small ? kTmaScratchWords : 0;
+    if (kind == kLaunchGeneral) return big + (small ? 1 : 0) > 1 ? kGeneralScratchWords : 0;
+    return 0;
+  }
+};
+
+// `next` continues the level chain of `prev` (its input is prev's last level).
+bool continues(const DispatchParams& prev, const DispatchParams& next) {
+  const LevelView& out = prev.lv[prev.levelCount];
+  return next.inputLevel == prev.inputLevel + prev.levelCount && next.lv[0].ptr == out.ptr &&
+         next.lv[0].pitch == out.pitch;
+}
+
+// Lower n dispatches to launches.  Small dispatches (smallDispatchSupported)
+// after a launch's large work run in that launch's last CTA; a run that
+// starts small is one single-CTA launch.  `fuse` false: one dispatch per
+// launch; `portableOnly`: every dispatch on the portable kernels.
+uint32_t planLaunches(const DispatchParams* p, uint32_t n, bool fuse, bool portableOnly, LaunchPlan* out) {
+  uint32_t count = 0;
+  // small dispatches continuing the chain from dispatch j on (at most `room`)
+  auto smallRun = [&](uint32_t j, uint32_t room) {
+    uint32_t k = j;
+    while (fuse && k < n && k - j < room && smallDispatchSupported(p[k]) && (k == j || continues(p[k - 1], p[k])))
+      ++k;
+    return k - j;
+  };
+  for (uint32_t i = 0; i < n;) {
+    LaunchPlan& l = out[count++];
+    l = LaunchPlan{kLaunchPortable, i, 1, 0};
+    if (portableOnly) {
+      i += 1;
+    } else if (smallDispatchSupported(p[i])) {
+      l.kind = kLaunchSmall;
+      l.big = 0;
+      l.small = fuse ? smallRun(i, kMaxSmallDispatches) : 1;
+      i += l.small;
+    } else if (p[i].isFast && tmaFastSupported(p[i])) {
+      l.kind = kLaunchTma;
+      l.small = smallRun(i + 1, kMaxSmallDispatches);
+      i += 1 + l.small;
+    } else if (generalFastSupported(p[i])) {
+      uint32_t j = i + 1;
+      while (fuse && j < n && j - i < generalMaxStages() && generalFastSupported(p[j]) &&
+             !smallDispatchSupported(p[j]) && p[j].sharedFmt == p[i].sharedFmt)
+        ++j;
+      l.kind = kLaunchGeneral;
+      l.big = j - i;
+      l.small = smallRun(j, kMaxSmallDispatches);
+      i = j + l.small;
+    } else {
+      i += 1;
+    }
+  }
+  return count;
+}
+
+// Enqueue one planned launch with the given scratch.
+cudaError_t runLaunch(const LaunchPlan& l, const DispatchParams* p, cudaStream_t s, const Scratch& scratch,
+                      uint32_t* launches, uint32_t debugFailCta = ~0u) {
+  const DispatchParams* d = p + l.first;
+  switch (l.kind) {
+    case kLaunchTma: return launchTmaFast(*d, l.small ? d + 1 : nullptr, l.small, s, scratch, launches, debugFailCta);
+    case kLaunchGeneral: return launchGeneralChain(d, l.big, d + l.big, l.small, s, scratch, launches);
+    case kLaunchSmall: return launchGeneralChain(d, 0, d, l.small, s, scratch, launches);
+    default: return launchPortable(*d, s, launches);
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -439,35 +518,14 @@ NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
   const bool fuse = !(cmd->flags & NVPRO_PYRAMID_CMD_NO_FUSION);
   // strided batches run on the portable kernels (one launch per dispatch, grid z = image)
   const bool portableOnly = (cmd->flags & NVPRO_PYRAMID_CMD_PORTABLE_KERNELS) != 0 || cmd->batch > 1;
-  size_t i = 0;
-  while (i < params.size()) {
-    const DispatchParams& p = params[i];
-    cudaError_t e;
-    if (!portableOnly && p.isFast && tmaFastSupported(p)) {
-      // Absorb following small dispatches of the same image into this
-      // kernel's tail (last-CTA-done), if every one of them is small.
-      size_t tail = 0;
-      if (fuse) {
-        size_t j = i + 1;
-        while (j < params.size() && j - i < tmaMaxFused() && tmaTailCompatible(params[j - 1], params[j])) ++j;
-        tail = j - i - 1;
-      }
-      e = launchTmaFast(p, tail ? &params[i + 1] : nullptr, uint32_t(tail), cmd->stream, cmd->scratch,
-                        &cmd->launches, cmd->debugFailNextTma ? 0u : ~0u);
-      cmd->debugFailNextTma = false;
-      i += 1 + tail;
-    } else if (!portableOnly && generalFastSupported(p)) {
-      // A run of general dispatches is one launch (fused unless NO_FUSION).
-      size_t j = i + 1;
-      while (fuse && j < params.size() && j - i < generalMaxStages() && generalFastSupported(params[j]) &&
-             params[j].sharedFmt == p.sharedFmt)
-        ++j;
-      e = launchGeneralChain(&params[i], uint32_t(j - i), cmd->stream, cmd->scratch, &cmd->launches);
-      i = j;
-    } else {
-      e = launchPortable(p, cmd->stream, &cmd->launches);
-      i += 1;
-    }
+  std::vector<LaunchPlan> plan(params.size());
+  plan.resize(planLaunches(params.data(), uint32_t(params.size()), fuse, portableOnly, plan.data()));
+  for (const LaunchPlan& l : plan) {
+    // the command's counters serve every launch: launches are stream-ordered
+    // and each leaves its counters at zero
+    const uint32_t failCta = (l.kind == kLaunchTma && cmd->debugFailNextTma) ? 0u : ~0u;
+    if (l.kind == kLaunchTma) cmd->debugFailNextTma = false;
+    const cudaError_t e = runLaunch(l, params.data(), cmd->stream, cmd->scratch, &cmd->launches, failCta);
     if (e != cudaSuccess)
       return fail(NVPRO_PYRAMID_ERROR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
   }
@@ -965,31 +1023,13 @@ NvproPyramidResult nvproPyramidGenerateNoAlloc(NvproPyramidStream stream, NvproP
 
   // Plan every launch and its words of the fixed array before enqueueing
   // anything, so a rejected chain leaves the stream untouched.
-  struct Launch {
-    uint32_t kind;  // 0 TMA fast kernel (+ fused tail), 1 general chain, 2 portable
-    uint32_t first, count, word;
-  };
-  Launch plan[NVPRO_PYRAMID_MAX_LEVELS];
-  uint32_t launchCount = 0, words = kStaticErrorWord + 1;
-  for (uint32_t i = 0; i < count;) {
-    const DispatchParams& p = params[i];
-    Launch& l = plan[launchCount++];
-    l.first = i;
-    l.word = words;
-    uint32_t j = i + 1;
-    if (p.isFast && tmaFastSupported(p)) {
-      while (j < count && j - i < tmaMaxFused() && tmaTailCompatible(params[j - 1], params[j])) ++j;
-      l.kind = 0;
-      words += kTmaScratchWords;
-    } else if (generalFastSupported(p)) {
-      while (j < count && j - i < generalMaxStages() && generalFastSupported(params[j])) ++j;
-      l.kind = 1;
-      words += kGeneralScratchWords;
-    } else {
-      l.kind = 2;
-    }
-    l.count = j - i;
-    i = j;
+  LaunchPlan plan[NVPRO_PYRAMID_MAX_LEVELS];
+  const uint32_t launchCount = planLaunches(params, count, true, false, plan);
+  uint32_t firstWord[NVPRO_PYRAMID_MAX_LEVELS];
+  uint32_t words = kStaticErrorWord + 1;
+  for (uint32_t k = 0; k < launchCount; ++k) {
+    firstWord[k] = words;
+    words += plan[k].words();
   }
   if (words > kStaticScratchWords)
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "chain needs %u of the %u fixed scratch words", words,
@@ -1000,22 +1040,13 @@ NvproPyramidResult nvproPyramidGenerateNoAlloc(NvproPyramidStream stream, NvproP
   cudaError_t e = staticScratch(&scratch);
   // Calls share the array and it keeps the last call's contents: the counters
   // start from zero; the error word stays until the status query reads it.
-  if (e == cudaSuccess)
+  if (e == cudaSuccess && words > kStaticErrorWord + 1)
     e = cudaMemsetAsync(scratch + kStaticErrorWord + 1, 0, (words - kStaticErrorWord - 1) * sizeof(uint32_t), s);
   if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "static scratch: %s", cudaGetErrorString(e));
   uint32_t launches = 0;
-  for (uint32_t k = 0; k < launchCount && e == cudaSuccess; ++k) {
-    const Launch& l = plan[k];
-    const DispatchParams& p = params[l.first];
-    if (l.kind == 0)
-      e = launchTmaFast(p, l.count > 1 ? &p + 1 : nullptr, l.count - 1, s,
-                        Scratch{scratch + l.word, kTmaScratchWords, scratch + kStaticErrorWord}, &launches);
-    else if (l.kind == 1)
-      e = launchGeneralChain(&p, l.count, s,
-                             Scratch{scratch + l.word, kGeneralScratchWords, scratch + kStaticErrorWord}, &launches);
-    else
-      e = launchPortable(p, s, &launches);
-  }
+  for (uint32_t k = 0; k < launchCount && e == cudaSuccess; ++k)
+    e = runLaunch(plan[k], params, s, Scratch{scratch + firstWord[k], plan[k].words(), scratch + kStaticErrorWord},
+                  &launches);
   if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
   return NVPRO_PYRAMID_SUCCESS;
 }

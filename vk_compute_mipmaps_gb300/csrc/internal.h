@@ -7,6 +7,10 @@
 namespace nvpyr {
 
 constexpr uint32_t kMaxDispatchLevels = 6;  // fast pipeline: 1..6 levels (nvpro_pyramid.glsl:221-225)
+// Dispatches whose input level has at most this many texels run on the
+// small-dispatch engine (small_engine.cuh), up to kMaxSmallDispatches per launch.
+constexpr uint32_t kSmallMaxTexels = 64 * 64;
+constexpr uint32_t kMaxSmallDispatches = 16;
 
 enum Preset : uint32_t { kSrgba8 = 1, kRgba32f = 2, kRgba16f = 3 };
 
@@ -69,15 +73,34 @@ struct Scratch {
   uint32_t* error() const { return errorFlag ? errorFlag : counters + kCounterError; }
 };
 
+// Workgroups of the reference's fast dispatcher that cover every 2^n tile of a
+// fast dispatch (nvpro_pyramid_dispatch.hpp:234-238: 4096 input samples per
+// group for 6 levels, else 1024).
+inline uint64_t fastGroupsNeeded(const DispatchParams& p) {
+  const uint32_t n = p.levelCount;
+  const uint64_t tiles = uint64_t(p.lv[0].w >> n) * (p.lv[0].h >> n);
+  const uint64_t perGroup = (n > 5 ? 4096u : 1024u) >> (2 * n);
+  const uint64_t per = perGroup ? perGroup : 1;
+  return (tiles + per - 1) / per;
+}
+
+// True if the dispatch's workgroups cover every texel it can write (the
+// default dispatchers always do; a caller's dispatcher may dispatch fewer).
+inline bool dispatchCoversAll(const DispatchParams& p) {
+  if (p.isBlit) return false;
+  if (p.isFast) return p.groups >= fastGroupsNeeded(p);
+  const LevelView &l1 = p.lv[1], &l2 = p.lv[2];
+  if (p.levelCount == 1) return p.groups * 128u >= uint64_t(l1.w) * l1.h;
+  return p.groups >= uint64_t((l2.w + 7) / 8) * ((l2.h + 7) / 8);
+}
+
 // Kernel families.  Each returns cudaSuccess or the launch error, and adds the
 // number of kernels it launched to *launches.
 cudaError_t launchPortable(const DispatchParams& p, cudaStream_t stream, uint32_t* launches);
 // True if the TMA fast-pipeline kernel can run this dispatch (layout, alignment).
 bool tmaFastSupported(const DispatchParams& p);
-// True if `next` may run inside the tail of the TMA kernel that runs `prev`.
-bool tmaTailCompatible(const DispatchParams& prev, const DispatchParams& next);
-// Maximum number of dispatches one TMA launch runs (itself plus its tail).
-uint32_t tmaMaxFused();
+// The TMA kernel runs dispatch p, then (its last CTA) the tailCount small
+// dispatches after it (smallDispatchSupported each, consecutive levels).
 // debugFailCta (test support): that CTA gives up at once, as after a wait
 // that ran out; ~0u = none.
 cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, uint32_t tailCount,
@@ -124,13 +147,18 @@ struct AdjointLevelParams {
 // (kernels_general.cu): dispatches of 1 or 2 levels whose input level is at
 // least 2x2 (and level L+1 too, for 2 levels) with full workgroup coverage.
 // A run of up to generalMaxStages() such dispatches is one cooperative launch
-// with grid barriers between them; for more than one dispatch it uses scratch
-// words kCounterError (or scratch.errorFlag), kCounterBarrier,
+// with grid barriers between them, followed by up to kMaxSmallDispatches small
+// dispatches that the last CTA runs; with no strip stages the launch is one
+// CTA running small dispatches only.  A launch of more than one part uses
+// scratch words kCounterError (or scratch.errorFlag), kCounterBarrier,
 // kCounterBarrierGen and kCounterExit.
 bool generalFastSupported(const DispatchParams& p);
 uint32_t generalMaxStages();
-cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStream_t stream, const Scratch& scratch,
-                               uint32_t* launches);
+cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, const DispatchParams* small,
+                               uint32_t smallCount, cudaStream_t stream, const Scratch& scratch, uint32_t* launches);
+// True if the small-dispatch engine runs p: sRGBA8, a dispatch (not a blit)
+// covering all its texels, one image, sizes within smallDispatchFits.
+bool smallDispatchSupported(const DispatchParams& p);
 
 // Premultiplied-alpha staging of sRGBA8 texels (kernels_stage.cu); src may equal dst.
 cudaError_t launchPremultiply(const uint8_t* src, uint64_t srcPitch, uint8_t* dst, uint64_t dstPitch, uint32_t width,

@@ -14,6 +14,7 @@
 #include <mutex>
 
 #include "general_strip.cuh"
+#include "small_engine.cuh"
 
 namespace nvpyr {
 namespace {
@@ -22,13 +23,15 @@ constexpr uint32_t kWarps = 12;
 constexpr uint32_t kThreads = 32 * kWarps;
 constexpr uint32_t kCtasPerSm = 1;
 constexpr uint32_t kMaxStages = 16;
-constexpr uint32_t kSmemBytes = kAlignedLutSmemBytes;
+// the aligned tables, then the small-dispatch engine's buffers
+constexpr uint32_t kSmemBytes = kAlignedLutSmemBytes + kSmallArenaBytes;
 static_assert(kCtasPerSm * (kSmemBytes + 1024u) <= 228u * 1024u, "the CTAs of an SM must fit");
 
 struct ChainParams {
-  Stage st[kMaxStages];
+  Stage st[kMaxStages];  // strip stages, all CTAs
   uint32_t stageCount;
-  uint32_t tailFrom;       // stages from here on are small: one CTA runs them
+  SmallDispatch tail[kMaxSmallDispatches];  // then small dispatches, one CTA
+  uint32_t tailCount;
   uint32_t* barrierCount;  // CTAs arrived at the current barrier (self-resetting)
   uint32_t* barrierGen;    // barrier generation (only ever incremented)
   uint32_t* errorFlag;     // set to 1 if a bounded wait gave up
@@ -67,26 +70,26 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint32_t okFlag;
   const Lut L = fillAlignedLut(smem, threadIdx.x, kThreads);
+  const bool multi = p.stageCount + (p.tailCount ? 1 : 0) > 1;  // uses the scratch counters
   uint32_t gen = 0;
   if (threadIdx.x == 0 && p.stageCount > 1) gen = ldAcquire(p.barrierGen);  // before this CTA's first arrival
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warpId = blockIdx.x * kWarps + (threadIdx.x >> 5), warps = gridDim.x * kWarps;
-  const uint32_t localWarp = threadIdx.x >> 5;
+  bool ok = true;
 #pragma unroll 1
   for (uint32_t s = 0; s < p.stageCount; ++s) {
-    const bool alone = s >= p.tailFrom;  // a small stage: this CTA alone
-    runStage<SF>(p.st[s], lane, alone ? localWarp : warpId, alone ? kWarps : warps, L);
-    if (s + 1 == p.stageCount) break;
-    if (s + 1 < p.tailFrom) {
-      if (!gridBarrier(p, gen, &okFlag)) break;
-    } else if (s + 1 == p.tailFrom) {
-      if (!lastCtaArrives(p.barrierCount, &okFlag)) break;  // the others are done
-    } else {
-      __syncthreads();  // the small stages: one CTA, block-level order
+    runStage<SF>(p.st[s], lane, warpId, warps, L);
+    if (s + 1 < p.stageCount && !gridBarrier(p, gen, &okFlag)) {
+      ok = false;
+      break;
     }
   }
-  if (p.stageCount > 1) exitArrive(p);
+  // the small dispatches: by the last CTA to finish the strips (a hand-off
+  // without waiting), or by the only CTA
+  if (ok && p.tailCount && (p.stageCount == 0 || lastCtaArrives(p.barrierCount, &okFlag)))
+    runSmallDispatches(p.tail, p.tailCount, smem + kAlignedLutSmemBytes, LutCodec{L}, threadIdx.x, kThreads);
+  if (multi) exitArrive(p);
 }
 
 // Test support for failure detection: one CTA arrives at the chain kernels'
@@ -158,11 +161,14 @@ void makeStage(const DispatchParams& p, uint64_t warpsResident, Stage* g) {
 bool generalFastSupported(const DispatchParams& p) {
   if (p.preset != kSrgba8 || p.isFast || p.isBlit || (p.levelCount != 1 && p.levelCount != 2)) return false;
   const LevelView &l0 = p.lv[0], &l1 = p.lv[1];
-  if (l0.w < 2 || l0.h < 2) return false;  // one-tap axes stay on the portable kernels
-  if (p.levelCount == 1) return p.groups * 128u >= uint64_t(l1.w) * l1.h;
-  const LevelView& l2 = p.lv[2];
-  if (l1.w < 2 || l1.h < 2) return false;
-  return p.groups >= uint64_t((l2.w + 7) / 8) * ((l2.h + 7) / 8);
+  if (l0.w < 2 || l0.h < 2) return false;  // one-tap axes: the small-dispatch engine or the portable kernels
+  if (p.levelCount == 2 && (l1.w < 2 || l1.h < 2)) return false;
+  return dispatchCoversAll(p);
+}
+
+bool smallDispatchSupported(const DispatchParams& p) {
+  return p.preset == kSrgba8 && !p.isBlit && p.batch <= 1 && p.levelCount >= 1 &&
+         p.levelCount <= kMaxDispatchLevels && dispatchCoversAll(p) && smallDispatchFits(p);
 }
 
 uint32_t generalMaxStages() { return kMaxStages; }
@@ -174,9 +180,11 @@ cudaError_t launchDebugGridBarrierTimeout(const Scratch& scratch, cudaStream_t s
   return cudaGetLastError();
 }
 
-cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStream_t stream, const Scratch& scratch,
-                               uint32_t* launches) {
-  if (count == 0 || count > kMaxStages || (count > 1 && scratch.counterCount < kGeneralScratchWords))
+cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, const DispatchParams* small,
+                               uint32_t smallCount, cudaStream_t stream, const Scratch& scratch, uint32_t* launches) {
+  const bool multi = count + (smallCount ? 1 : 0) > 1;
+  if (count + smallCount == 0 || count > kMaxStages || smallCount > kMaxSmallDispatches ||
+      (multi && scratch.counterCount < kGeneralScratchWords))
     return cudaErrorInvalidValue;
   for (uint32_t i = 1; i < count; ++i)
     if (p[i].sharedFmt != p[0].sharedFmt) return cudaErrorInvalidValue;  // one shared format per launch
@@ -191,27 +199,20 @@ cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, cudaStre
     makeStage(p[i], uint64_t(ctas) * kWarps, &cp.st[i]);
     maxUnits = std::max<uint64_t>(maxUnits, uint64_t(cp.st[i].tilesX) * cp.st[i].bands);
   }
-  // Stages whose input has at most 64 x 64 texels go to one CTA after the
-  // last larger one (a grid barrier costs more than their work); a chain of
-  // only such stages is one CTA from the start (measured: 2560x1440, whose
-  // general run starts on 80x45, 43.0 -> 39.9 us against a 64-per-side rule;
-  // 128 x 128 texels made 2047^2 slower).
-  cp.tailFrom = count;
-  while (cp.tailFrom > 0 && uint64_t(p[cp.tailFrom - 1].lv[0].w) * p[cp.tailFrom - 1].lv[0].h <= 64u * 64u)
-    --cp.tailFrom;
-  for (uint32_t i = cp.tailFrom; i < count; ++i) makeStage(p[i], kWarps, &cp.st[i]);  // bands for one CTA
-  if (count > 1) {
+  cp.tailCount = smallCount;
+  for (uint32_t i = 0; i < smallCount; ++i) makeSmallDispatch(small[i], &cp.tail[i]);
+  if (multi) {
     cp.barrierCount = scratch.counters + kCounterBarrier;
     cp.barrierGen = scratch.counters + kCounterBarrierGen;
     cp.errorFlag = scratch.error();
     cp.exitCount = scratch.counters + kCounterExit;
   }
-  // a single stage needs no more CTAs than its strips fill; small stages only: one
+  // a single stage needs no more CTAs than its strips fill; small dispatches only: one
   uint32_t grid = count > 1 ? ctas : uint32_t(std::min<uint64_t>((maxUnits + kWarps - 1) / kWarps, ctas));
-  if (cp.tailFrom == 0) grid = 1;
+  if (count == 0) grid = 1;
   void* args[] = {&cp};
-  e = cudaLaunchCooperativeKernel(chainKernel(p[0].sharedFmt), dim3(grid),
-                                  dim3(kThreads), args, kSmemBytes, stream);
+  const uint32_t fmt = count ? p[0].sharedFmt : kSharedFp32;  // the engine applies each dispatch's own format
+  e = cudaLaunchCooperativeKernel(chainKernel(fmt), dim3(grid), dim3(kThreads), args, kSmemBytes, stream);
   if (e != cudaSuccess) return e;
   ++*launches;
   return cudaSuccess;

@@ -33,22 +33,23 @@
 // comparison against the exact threshold table (also replicated per lane);
 // the result equals the exact threshold count for every x in [0, 1].
 //
-// Tail fusion.  When the dispatches after this one are small fast
-// dispatches of the same image (single 64x64 regions, e.g. the F6 of a 64x64
-// level after the first F6 of 4096^2),
-// every CTA increments a counter after its regions; the last CTA (it sees
-// count == gridDim.x - 1 after a release/acquire fence pair) runs those
-// dispatches itself, reading the freshly written level with L2-coherent
-// loads.  No thread waits on another CTA, so there is no spin on a flag.
-// Every CTA arrives, also one whose bounded wait gave up (it then marks its
-// arrival as failed and the last CTA skips the tail), so the counter is back
-// at zero when the kernel ends, whatever happened.
+// Trailing dispatches.  The small dispatches after this one (input levels of
+// at most kSmallMaxTexels texels, fast or general: e.g. the F6 of the 64x64
+// level after the first F6 of 4096^2, or everything after the F5 of
+// 2560x1440) run in the same launch: every CTA increments a counter after
+// its regions; the last CTA (it sees the count reach gridDim.x after a
+// release/acquire fence pair) runs them with the small-dispatch engine
+// (small_engine.cuh) in the freed region buffers.  No thread waits on another
+// CTA, so there is no spin on a flag.  Every CTA arrives, also one whose
+// bounded wait gave up (it then marks its arrival as failed and the last CTA
+// skips the tail), so the counter is back at zero when the kernel ends,
+// whatever happened.
 #include <cuda.h>
 
 #include <atomic>
 #include <mutex>
 
-#include "srgb_codec.cuh"
+#include "small_engine.cuh"
 
 namespace nvpyr {
 namespace {
@@ -63,7 +64,6 @@ constexpr uint32_t kThreads = kConsumerThreads + 32 * kGroups;
 constexpr uint32_t kStages = 2;
 constexpr uint32_t kXchgRing = 2;
 constexpr uint32_t kTileBytes = kTile * kTile * 4;
-constexpr uint32_t kMaxFused = 4;
 // Bounded mbarrier waits: each try_wait carries a suspend-time hint, so a
 // waiting warp is parked by the hardware until the phase completes (or the
 // hint runs out) instead of polling.  After about a second of %globaltimer
@@ -88,6 +88,7 @@ constexpr uint32_t kIssuedOff = kBarOff + kGroups * kBarsPerGroup * 8;  // [grou
 constexpr uint32_t kSmemBytes = kIssuedOff + kGroups * kStages * 4;
 static_assert(kStageOff % 128 == 0, "TMA destinations need 128-byte alignment");
 static_assert(kSmemBytes <= 232448, "exceeds the 227 KiB of shared memory per CTA");
+static_assert(kSmallArenaBytes <= kGroups * kStages * kTileBytes, "the tail runs in the region buffers");
 constexpr uint32_t kDebugSmemBytes = kLutThrOff + kThrRows * 128;
 
 struct FusedStage {
@@ -101,8 +102,9 @@ struct FusedStage {
 };
 
 struct TmaParams {
-  FusedStage st[kMaxFused];
-  uint32_t stageCount;
+  FusedStage st;                            // the dispatch over the TMA-loaded level
+  SmallDispatch tail[kMaxSmallDispatches];  // the small dispatches after it
+  uint32_t tailCount;
   uint32_t* counter;    // last-CTA-done counter (self-resetting)
   uint32_t* errorFlag;  // set to 1 if a bounded wait gave up
   // Test support: this CTA gives up at once, as if its first wait had run out
@@ -114,10 +116,6 @@ __device__ __forceinline__ Lut makeLut(uint32_t lane) {
   extern __shared__ __align__(128) uint8_t smem[];
   const uint32_t base = smemAddr(smem);
   return makeLutAt(base + kLutDecodeOff, base + kLutThrOff, lane);
-}
-
-__device__ __forceinline__ void groupSync(uint32_t g) {
-  asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(kGroupThreads) : "memory");
 }
 
 // Low 32 bits of the nanosecond global timer (wraps every ~4.3 s; the
@@ -424,49 +422,6 @@ __device__ __forceinline__ bool mainLoopN(const FusedStage& st, const CUtensorMa
   }
 }
 
-// One region of a tail dispatch: buffer filled with plain loads, group
-// barriers around the shared steps (the tail is a few regions at most).
-template <uint32_t N, uint32_t SF>
-__device__ __forceinline__ void tailRegion(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
-                                           float4* xchg, uint32_t g, uint32_t wig, uint32_t lane, uint32_t it,
-                                           const Lut& L) {
-  // the tail is a few regions: always bounds-checked
-  float4 c0 = make_float4(0, 0, 0, 0), c1 = c0;
-  levels12<N, true>(st, x0, y0, tile, wig, lane, L, c0, c1);
-  levels34<N, SF, true>(st, x0, y0, c0, c1, xchg, wig, lane, L);
-  groupSync(g);
-  if (N >= 5 && wig == (it & 3)) finishTop<N, true>(st, x0, y0, xchg, lane, L);
-}
-
-template <uint32_t SF>
-__device__ __forceinline__ void tailRegionN(const FusedStage& st, uint32_t x0, uint32_t y0, const uint32_t* tile,
-                                            float4* xchg, uint32_t g, uint32_t wig, uint32_t lane, uint32_t it,
-                                            const Lut& L) {
-  switch (st.n) {
-    case 1: tailRegion<1, kFmtOf<1, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 2: tailRegion<2, kFmtOf<2, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 3: tailRegion<3, kFmtOf<3, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 4: tailRegion<4, kFmtOf<4, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    case 5: tailRegion<5, kFmtOf<5, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-    default: tailRegion<6, kFmtOf<6, SF>>(st, x0, y0, tile, xchg, g, wig, lane, it, L); break;
-  }
-}
-
-// Fill a region buffer from global memory with L2-coherent loads (tail
-// dispatches read a level written earlier in this kernel).  Texels outside
-// the covered extent are zero, as the TMA fill would give.
-__device__ __forceinline__ void loadRegionPlain(const FusedStage& st, uint32_t x0, uint32_t y0, uint32_t* tile,
-                                                uint32_t gtid) {
-  for (uint32_t i = gtid; i < kTile * kTile; i += kGroupThreads) {
-    const uint32_t x = i % kTile, y = i / kTile;
-    uint32_t v = 0;
-    if (x0 + x < st.coverW && y0 + y < st.coverH)
-      v = __ldcg(reinterpret_cast<const unsigned int*>(st.src + uint64_t(y0 + y) * st.srcPitch +
-                                                       uint64_t(x0 + x) * 4));
-    tile[i] = v;
-  }
-}
-
 // SF: the fast pipeline's shared format (the same for every stage of a launch).
 template <uint32_t SF>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -501,7 +456,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
-  const FusedStage& s0 = p.st[0];
+  const FusedStage& s0 = p.st;
   const uint32_t regions = s0.regionsX * s0.regionsY;
   const uint32_t groupsTotal = gridDim.x * kGroups;
   if (warp >= kProducerWarp0 && lane == 0) {  // the first two regions of the group
@@ -530,7 +485,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (G.issued[s]) mbarWait(G.full0 + 8 * s, (G.issued[s] - 1) & 1);
     }
   }
-  if (p.stageCount < 2) return;
+  if (p.tailCount == 0) return;
 
   // ---- last CTA runs the trailing dispatches ----
   // Every CTA arrives, a failed one with kFailedArrival added, so the counter
@@ -547,23 +502,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       last = total < kFailedArrival;
     }
   }
-  if (!__syncthreads_or(last) || warp >= kProducerWarp0) return;
-  const uint32_t g = warp / kGroupWarps, wig = warp % kGroupWarps, gtid = tid % kGroupThreads;
-  const GroupCtx G = groupCtx(g);
-  uint32_t* tile = const_cast<uint32_t*>(G.tiles);
-  for (uint32_t d = 1; d < p.stageCount; ++d) {
-    const FusedStage& st = p.st[d];
-    const uint32_t nreg = st.regionsX * st.regionsY;
-    for (uint32_t r = g, it = 0; r < nreg; r += kGroups, ++it) {
-      const uint32_t x0 = (r % st.regionsX) * kTile, y0 = (r / st.regionsX) * kTile;
-      loadRegionPlain(st, x0, y0, tile, gtid);
-      groupSync(g);
-      tailRegionN<SF>(st, x0, y0, tile, G.xchg + (it % kXchgRing) * 16, g, wig, lane, it, L);
-      groupSync(g);
-    }
-    // consumer warps only (the producer warps have left)
-    asm volatile("bar.sync 5, %0;" ::"r"(kConsumerThreads) : "memory");
-  }
+  if (!__syncthreads_or(last)) return;
+  // every thread of the CTA, the producer warps too, in the freed region buffers
+  runSmallDispatches(p.tail, p.tailCount, smem + kStageOff, LutCodec{L}, tid, kThreads);
 }
 
 // Test support for failure detection: one warp waits, with the kernels' own
@@ -670,13 +611,6 @@ cudaError_t deviceInfo(DeviceInfo** out) {
   return cudaSuccess;
 }
 
-uint64_t fastGroupsNeeded(const DispatchParams& p) {
-  const uint32_t n = p.levelCount;
-  const uint64_t tiles = uint64_t(p.lv[0].w >> n) * (p.lv[0].h >> n);
-  const uint64_t perGroup = std::max<uint64_t>((n > 5 ? 4096u : 1024u) >> (2 * n), 1);
-  return (tiles + perGroup - 1) / perGroup;
-}
-
 void fillStage(const DispatchParams& p, FusedStage* st) {
   const uint32_t n = p.levelCount;
   st->n = n;
@@ -706,37 +640,18 @@ bool tmaFastSupported(const DispatchParams& p) {
   return encodeTiled() != nullptr;
 }
 
-bool tmaTailCompatible(const DispatchParams& prev, const DispatchParams& next) {
-  if (next.preset != kSrgba8 || !next.isFast || next.levelCount < 1 || next.levelCount > 6) return false;
-  if (next.inputLevel != prev.inputLevel + prev.levelCount || next.sharedFmt != prev.sharedFmt) return false;
-  if (next.lv[0].ptr != prev.lv[prev.levelCount].ptr || next.lv[0].pitch != prev.lv[prev.levelCount].pitch)
-    return false;
-  if ((next.lv[0].w >> next.levelCount) == 0 || (next.lv[0].h >> next.levelCount) == 0) return false;
-  if (reinterpret_cast<uintptr_t>(next.lv[1].ptr) % 8 || next.lv[1].pitch % 8 ||
-      ((next.lv[0].w >> next.levelCount) << next.levelCount) % 4)
-    return false;
-  if (next.groups < fastGroupsNeeded(next)) return false;
-  // One CTA runs the tail, region after region: fuse a dispatch of a single
-  // region only.  (A 256x256 input -- 16 regions -- took ~75 us in the last
-  // CTA against a few us as its own launch over 16 CTAs.)
-  return next.lv[0].w <= kTile && next.lv[0].h <= kTile;
-}
-
-uint32_t tmaMaxFused() { return kMaxFused; }
-
 cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, uint32_t tailCount,
                           cudaStream_t stream, const Scratch& scratch, uint32_t* launches, uint32_t debugFailCta) {
   DeviceInfo* info = nullptr;
   cudaError_t e = deviceInfo(&info);
   if (e != cudaSuccess) return e;
-  if (tailCount + 1 > kMaxFused || (tailCount && scratch.counterCount < kTmaScratchWords))
+  if (tailCount > kMaxSmallDispatches || (tailCount && scratch.counterCount < kTmaScratchWords))
     return cudaErrorInvalidValue;
-  for (uint32_t i = 0; i < tailCount; ++i)
-    if (tail[i].sharedFmt != p.sharedFmt) return cudaErrorInvalidValue;  // one shared format per launch
+  // the tail's dispatches carry their own shared formats (the engine applies them)
   TmaParams tp{};
-  fillStage(p, &tp.st[0]);
-  for (uint32_t i = 0; i < tailCount; ++i) fillStage(tail[i], &tp.st[i + 1]);
-  tp.stageCount = 1 + tailCount;
+  fillStage(p, &tp.st);
+  for (uint32_t i = 0; i < tailCount; ++i) makeSmallDispatch(tail[i], &tp.tail[i]);
+  tp.tailCount = tailCount;
   tp.counter = scratch.counters;
   tp.errorFlag = scratch.counters ? scratch.error() : nullptr;
   tp.failCta = tp.errorFlag ? debugFailCta : ~0u;
@@ -750,7 +665,7 @@ cudaError_t launchTmaFast(const DispatchParams& p, const DispatchParams* tail, u
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS) return cudaErrorInvalidValue;
-  const uint64_t regions = uint64_t(tp.st[0].regionsX) * tp.st[0].regionsY;
+  const uint64_t regions = uint64_t(tp.st.regionsX) * tp.st.regionsY;
   const uint32_t grid = uint32_t(std::min<uint64_t>(regions, uint64_t(info->sms)));
   void* args[] = {&map, &tp};
   cudaLaunchConfig_t cfg = {};
