@@ -402,6 +402,15 @@ __device__ __forceinline__ bool lastCtaArrives(uint32_t* count, uint32_t* flag) 
   return *flag != 0;
 }
 
+// The sRGB codec through the tables of fillAlignedLut: the decode table's
+// address comes whole from the PRMT (decodeAligned), since the Lut's lane word
+// carries the table's upper address bytes.
+struct AlignedLutCodec {
+  Lut L;
+  __device__ __forceinline__ float4 decode(uint32_t w) const { return decodeAligned(w, L); }
+  __device__ __forceinline__ uint32_t encode(float4 v) const { return encodeTexel(v, L); }
+};
+
 // Fill the aligned tables in `smem` (kAlignedLutSmemBytes of dynamic shared
 // memory) and return the lane's table constants.  Call with every thread of
 // the CTA; a __syncthreads must follow before the first lookup.

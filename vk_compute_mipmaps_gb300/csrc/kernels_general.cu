@@ -88,7 +88,8 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
   // the small dispatches: by the last CTA to finish the strips (a hand-off
   // without waiting), or by the only CTA
   if (ok && p.tailCount && (p.stageCount == 0 || lastCtaArrives(p.barrierCount, &okFlag)))
-    runSmallDispatches(p.tail, p.tailCount, smem + kAlignedLutSmemBytes, LutCodec{L}, threadIdx.x, kThreads);
+    runSmallDispatches(p.tail, p.tailCount, smem + kAlignedLutSmemBytes, AlignedLutCodec{L}, threadIdx.x,
+                       kThreads);
   if (multi) exitArrive(p);
 }
 

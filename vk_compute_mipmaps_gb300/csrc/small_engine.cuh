@@ -42,7 +42,8 @@ constexpr uint32_t kSmallL1Texels = kSmallMaxTexels / 4;
 constexpr uint32_t kSmallL2Texels = kSmallMaxTexels / 16;
 constexpr uint32_t kSmallArenaBytes = 16 * (kSmallL1Texels + kSmallL2Texels) + 2 * 4 * kSmallL1Texels;
 
-// The sRGB codec through the replicated tables of a Lut (either layout).
+// The sRGB codec through the replicated tables of a Lut made by makeLutAt
+// (the TMA kernel's layout).
 struct LutCodec {
   Lut L;
   __device__ __forceinline__ float4 decode(uint32_t w) const { return decodeTexel(w, L); }
