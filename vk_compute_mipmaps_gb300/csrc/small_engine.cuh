@@ -34,13 +34,14 @@ struct SmallDispatch {
 };
 
 // Shared memory of the engine: FP32 levels L+1 and L+2 of a dispatch, and two
-// code buffers (the output level of the previous dispatch, of this one).  A
-// dispatch fits if level L+1 has at most kSmallL1Texels texels and level L+2
-// at most kSmallL2Texels (always, for levels at least four texels on each
-// side; see smallDispatchFits).
+// code buffers: the input level of the run (kSmallMaxTexels codes, loaded from
+// global memory at the start) and the output level of a dispatch, which
+// alternate between dispatches.  A dispatch fits if level L+1 has at most
+// kSmallL1Texels texels and level L+2 at most kSmallL2Texels (always, for
+// levels at least four texels on each side; see smallDispatchFits).
 constexpr uint32_t kSmallL1Texels = kSmallMaxTexels / 4;
 constexpr uint32_t kSmallL2Texels = kSmallMaxTexels / 16;
-constexpr uint32_t kSmallArenaBytes = 16 * (kSmallL1Texels + kSmallL2Texels) + 2 * 4 * kSmallL1Texels;
+constexpr uint32_t kSmallArenaBytes = 16 * (kSmallL1Texels + kSmallL2Texels) + 4 * (kSmallMaxTexels + kSmallL1Texels);
 
 // The sRGB codec through the replicated tables of a Lut made by makeLutAt
 // (the TMA kernel's layout).
@@ -54,82 +55,133 @@ __device__ __forceinline__ uint32_t ldcgTexel(const uint8_t* p) {
   return __ldcg(reinterpret_cast<const unsigned int*>(p));
 }
 
+// Input texel (x, y) of a level step: a stored code (decoded) or an FP32
+// value handed on inside the dispatch.
+template <bool CODES, typename Codec>
+__device__ __forceinline__ float4 smallIn(const uint32_t* codes, const float4* vals, uint32_t w, uint32_t x,
+                                          uint32_t y, const Codec& C) {
+  return CODES ? C.decode(codes[y * w + x]) : vals[y * w + x];
+}
+
+// One level of a dispatch: level k (wk x hk) from level k-1 (wi x hi), every
+// texel stored to global memory, and kept as a code (last level of the
+// dispatch) or as an FP32 value (after the shared format at the hand-off level).
+template <bool CODES, bool FAST, typename Codec>
+__device__ __forceinline__ void smallLevel(const uint32_t* inCodes, const float4* inVals, uint32_t wi, uint32_t hi,
+                                           uint32_t wk, uint32_t hk, bool vert, uint8_t* dst, uint64_t pitch,
+                                           uint32_t* outCodes, float4* outVals, bool handoff, uint32_t sharedFmt,
+                                           const Codec& C, uint32_t tid, uint32_t nthreads) {
+  const uint32_t kx = kernelSize(wi), ky = kernelSize(hi);
+  for (uint32_t t = tid; t < wk * hk; t += nthreads) {
+    const uint32_t y = t / wk, x = t - y * wk;
+    float4 v;
+    if (FAST) {
+      const float4 tl = smallIn<CODES>(inCodes, inVals, wi, 2 * x, 2 * y, C);
+      const float4 tr = smallIn<CODES>(inCodes, inVals, wi, 2 * x + 1, 2 * y, C);
+      const float4 bl = smallIn<CODES>(inCodes, inVals, wi, 2 * x, 2 * y + 1, C);
+      const float4 br = smallIn<CODES>(inCodes, inVals, wi, 2 * x + 1, 2 * y + 1, C);
+      v = fastReduce(vert, tl, tr, bl, br);
+    } else {
+      // kernel size 1 reads row / column 0 only; 2 and 3 their taps
+      const uint32_t y1 = ky > 1 ? 2 * y + 1 : 2 * y, y2 = ky > 2 ? 2 * y + 2 : 2 * y;
+      const Weights3 wy = weights3(hk, y);
+      float4 h[3];
+#pragma unroll
+      for (uint32_t c = 0; c < 3; ++c) {
+        const uint32_t xc = 2 * x + (c < kx ? c : 0);
+        const float4 a = smallIn<CODES>(inCodes, inVals, wi, xc, 2 * y, C);
+        const float4 b = smallIn<CODES>(inCodes, inVals, wi, xc, y1, C);
+        const float4 e = smallIn<CODES>(inCodes, inVals, wi, xc, y2, C);
+        h[c] = ky == 3 ? reduce3(wy.w0, a, wy.w1, b, wy.w2, e) : ky == 2 ? reduce2(a, b) : a;
+      }
+      if (kx == 3) {
+        const Weights3 wx = weights3(wk, x);
+        v = reduce3(wx.w0, h[0], wx.w1, h[1], wx.w2, h[2]);
+      } else {
+        v = kx == 2 ? reduce2(h[0], h[1]) : h[0];
+      }
+    }
+    const uint32_t code = C.encode(v);
+    *reinterpret_cast<uint32_t*>(dst + uint64_t(y) * pitch + uint64_t(x) * 4) = code;
+    if (outCodes) {
+      outCodes[t] = code;
+    } else {
+      if (handoff) {
+        if (sharedFmt == kSharedSrgb) v = C.decode(code);
+        else if (sharedFmt == kSharedF16) v = f16RoundTrip(v);
+      }
+      outVals[t] = v;
+    }
+  }
+}
+
 template <typename Codec>
 __device__ __noinline__ void runSmallDispatches(const SmallDispatch* ds, uint32_t count, uint8_t* arena,
-                                                const Codec& C, uint32_t tid, uint32_t nthreads) {
+                                                const Codec C, uint32_t tid, uint32_t nthreads) {
   float4* const bufA = reinterpret_cast<float4*>(arena);
   float4* const bufB = bufA + kSmallL1Texels;
-  uint32_t* const codes0 = reinterpret_cast<uint32_t*>(bufB + kSmallL2Texels);
-  uint32_t* const codes1 = codes0 + kSmallL1Texels;
-  const uint32_t* inCodes = nullptr;  // output codes of the previous dispatch
-#pragma unroll 1
-  for (uint32_t i = 0; i < count; ++i) {
-    const SmallDispatch d = ds[i];
-    const uint32_t handoff = sharedHandoffLevel(d.isFast != 0, d.n);
-    uint32_t* const outCodes = (i & 1) ? codes1 : codes0;
-    uint32_t wi = d.w0, hi = d.h0;
-    const float4* inF = nullptr;
-#pragma unroll 1
-    for (uint32_t k = 1; k <= d.n; ++k) {
-      const uint32_t wk = max(wi >> 1, 1u), hk = max(hi >> 1, 1u);
-      float4* const outF = k < d.n ? ((k & 1) ? bufA : bufB) : nullptr;
-      const uint32_t kx = kernelSize(wi), ky = kernelSize(hi);
-      const bool vert = fastVerticalFirst(d.n, k);
-      uint8_t* const dst = d.dst[k - 1];
-      const uint64_t pitch = d.pitch[k - 1];
-      auto in = [&](uint32_t x, uint32_t y) -> float4 {
-        if (inF) return inF[y * wi + x];
-        return C.decode(inCodes ? inCodes[y * wi + x]
-                                : ldcgTexel(d.src + uint64_t(y) * d.srcPitch + uint64_t(x) * 4));
-      };
-      for (uint32_t t = tid; t < wk * hk; t += nthreads) {
-        const uint32_t x = t % wk, y = t / wk;
-        float4 v;
-        if (d.isFast) {
-          v = fastReduce(vert, in(2 * x, 2 * y), in(2 * x + 1, 2 * y), in(2 * x, 2 * y + 1),
-                         in(2 * x + 1, 2 * y + 1));
-        } else {
-          float4 h[3];
+  uint32_t* const codesIn = reinterpret_cast<uint32_t*>(bufB + kSmallL2Texels);  // kSmallMaxTexels
+  uint32_t* const codesOut = codesIn + kSmallMaxTexels;                          // kSmallL1Texels
+  // The run's input level into shared memory, eight loads in flight per thread.
+  {
+    const uint32_t w0 = ds[0].w0, n0 = w0 * ds[0].h0;
+    const uint8_t* const src = ds[0].src;
+    const uint64_t srcPitch = ds[0].srcPitch;
+    for (uint32_t t0 = tid; t0 < n0; t0 += 8 * nthreads) {
+      uint32_t v[8];
 #pragma unroll
-          for (uint32_t c = 0; c < 3; ++c) {
-            if (c >= kx) break;
-            if (ky == 3) {
-              const Weights3 w = weights3(hk, y);
-              h[c] = reduce3(w.w0, in(2 * x + c, 2 * y), w.w1, in(2 * x + c, 2 * y + 1), w.w2,
-                             in(2 * x + c, 2 * y + 2));
-            } else if (ky == 2) {
-              h[c] = reduce2(in(2 * x + c, 2 * y), in(2 * x + c, 2 * y + 1));
-            } else {
-              h[c] = in(2 * x + c, 2 * y);
-            }
-          }
-          if (kx == 3) {
-            const Weights3 w = weights3(wk, x);
-            v = reduce3(w.w0, h[0], w.w1, h[1], w.w2, h[2]);
-          } else if (kx == 2) {
-            v = reduce2(h[0], h[1]);
-          } else {
-            v = h[0];
-          }
-        }
-        const uint32_t code = C.encode(v);
-        *reinterpret_cast<uint32_t*>(dst + uint64_t(y) * pitch + uint64_t(x) * 4) = code;
-        if (k == d.n) {
-          outCodes[t] = code;
-        } else {
-          if (k == handoff) {
-            if (d.sharedFmt == kSharedSrgb) v = C.decode(code);
-            else if (d.sharedFmt == kSharedF16) v = f16RoundTrip(v);
-          }
-          outF[t] = v;
+      for (uint32_t j = 0; j < 8; ++j) {
+        const uint32_t t = t0 + j * nthreads;
+        if (t < n0) {
+          const uint32_t y = t / w0;
+          v[j] = ldcgTexel(src + uint64_t(y) * srcPitch + uint64_t(t - y * w0) * 4);
         }
       }
+#pragma unroll
+      for (uint32_t j = 0; j < 8; ++j)
+        if (t0 + j * nthreads < n0) codesIn[t0 + j * nthreads] = v[j];
+    }
+  }
+  __syncthreads();
+  // the input codes of dispatch i, its output codes (they alternate)
+  uint32_t* in = codesIn;
+  uint32_t* out = codesOut;
+#pragma unroll 1
+  for (uint32_t i = 0; i < count; ++i) {
+    const uint32_t isFast = ds[i].isFast, n = ds[i].n, sharedFmt = ds[i].sharedFmt;
+    const uint32_t handoff = sharedHandoffLevel(isFast != 0, n);
+    uint32_t wi = ds[i].w0, hi = ds[i].h0;
+#pragma unroll 1
+    for (uint32_t k = 1; k <= n; ++k) {
+      const uint32_t wk = max(wi >> 1, 1u), hk = max(hi >> 1, 1u);
+      float4* const outVals = k < n ? ((k & 1) ? bufA : bufB) : nullptr;
+      const float4* const inVals = (k & 1) ? bufB : bufA;  // level k-1's values (k >= 2)
+      uint32_t* const outCodes = k == n ? out : nullptr;
+      const bool vert = fastVerticalFirst(n, k);
+      uint8_t* const dst = ds[i].dst[k - 1];
+      const uint64_t pitch = ds[i].pitch[k - 1];
+      if (k == 1) {
+        if (isFast)
+          smallLevel<true, true>(in, inVals, wi, hi, wk, hk, vert, dst, pitch, outCodes, outVals, k == handoff,
+                                 sharedFmt, C, tid, nthreads);
+        else
+          smallLevel<true, false>(in, inVals, wi, hi, wk, hk, vert, dst, pitch, outCodes, outVals, k == handoff,
+                                  sharedFmt, C, tid, nthreads);
+      } else {
+        if (isFast)
+          smallLevel<false, true>(in, inVals, wi, hi, wk, hk, vert, dst, pitch, outCodes, outVals, k == handoff,
+                                  sharedFmt, C, tid, nthreads);
+        else
+          smallLevel<false, false>(in, inVals, wi, hi, wk, hk, vert, dst, pitch, outCodes, outVals,
+                                   k == handoff, sharedFmt, C, tid, nthreads);
+      }
       __syncthreads();
-      inF = outF;
       wi = wk;
       hi = hk;
     }
-    inCodes = outCodes;
+    uint32_t* const t = in;  // swap: this output is the next input (later levels fit either buffer)
+    in = out;
+    out = t;
   }
 }
 
