@@ -55,6 +55,13 @@ __device__ __forceinline__ uint32_t ldcgTexel(const uint8_t* p) {
   return __ldcg(reinterpret_cast<const unsigned int*>(p));
 }
 
+// floor(t / w) for t < 2^20 as a multiply-high by r = recip32(w) = floor((2^32 - 1) / w) + 1:
+// t * r / 2^32 exceeds t / w by less than t / 2^32, less than the distance to the next integer.
+__device__ __forceinline__ uint32_t recip32(uint32_t w) { return 0xFFFFFFFFu / w + 1u; }
+__device__ __forceinline__ uint32_t divBy(uint32_t t, uint32_t r, uint32_t w) {
+  return w == 1 ? t : __umulhi(t, r);
+}
+
 // Input texel (x, y) of a level step: a stored code (decoded) or an FP32
 // value handed on inside the dispatch.
 template <bool CODES, typename Codec>
@@ -72,8 +79,9 @@ __device__ __forceinline__ void smallLevel(const uint32_t* inCodes, const float4
                                            uint32_t* outCodes, float4* outVals, bool handoff, uint32_t sharedFmt,
                                            const Codec& C, uint32_t tid, uint32_t nthreads) {
   const uint32_t kx = kernelSize(wi), ky = kernelSize(hi);
+  const uint32_t r = recip32(wk);
   for (uint32_t t = tid; t < wk * hk; t += nthreads) {
-    const uint32_t y = t / wk, x = t - y * wk;
+    const uint32_t y = divBy(t, r, wk), x = t - y * wk;
     float4 v;
     if (FAST) {
       const float4 tl = smallIn<CODES>(inCodes, inVals, wi, 2 * x, 2 * y, C);
@@ -116,7 +124,7 @@ __device__ __forceinline__ void smallLevel(const uint32_t* inCodes, const float4
 }
 
 template <typename Codec>
-__device__ __noinline__ void runSmallDispatches(const SmallDispatch* ds, uint32_t count, uint8_t* arena,
+__device__ __forceinline__ void runSmallDispatches(const SmallDispatch* ds, uint32_t count, uint8_t* arena,
                                                 const Codec C, uint32_t tid, uint32_t nthreads) {
   float4* const bufA = reinterpret_cast<float4*>(arena);
   float4* const bufB = bufA + kSmallL1Texels;
@@ -124,7 +132,7 @@ __device__ __noinline__ void runSmallDispatches(const SmallDispatch* ds, uint32_
   uint32_t* const codesOut = codesIn + kSmallMaxTexels;                          // kSmallL1Texels
   // The run's input level into shared memory, eight loads in flight per thread.
   {
-    const uint32_t w0 = ds[0].w0, n0 = w0 * ds[0].h0;
+    const uint32_t w0 = ds[0].w0, n0 = w0 * ds[0].h0, r0 = recip32(w0);
     const uint8_t* const src = ds[0].src;
     const uint64_t srcPitch = ds[0].srcPitch;
     for (uint32_t t0 = tid; t0 < n0; t0 += 8 * nthreads) {
@@ -133,7 +141,7 @@ __device__ __noinline__ void runSmallDispatches(const SmallDispatch* ds, uint32_
       for (uint32_t j = 0; j < 8; ++j) {
         const uint32_t t = t0 + j * nthreads;
         if (t < n0) {
-          const uint32_t y = t / w0;
+          const uint32_t y = divBy(t, r0, w0);
           v[j] = ldcgTexel(src + uint64_t(y) * srcPitch + uint64_t(t - y * w0) * 4);
         }
       }
