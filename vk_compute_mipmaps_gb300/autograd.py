@@ -40,21 +40,6 @@ def _check_base(base: torch.Tensor):
         raise ValueError("base must be a CUDA tensor of shape [B, H, W, 4] or [H, W, 4]")
 
 
-_geometry_cache: dict = {}
-
-
-def _geometry(W: int, H: int, levels: int, esz: int):
-    """Per (W, H, levels, element size): the level sizes and the per-image
-    byte stride of every level (cached: the same for every call of a
-    training loop)."""
-    key = (W, H, levels, esz)
-    g = _geometry_cache.get(key)
-    if g is None:
-        sizes = level_sizes(W, H, levels)
-        g = _geometry_cache[key] = (sizes, _strides(sizes, esz))
-    return g
-
-
 def _strides(sizes, esz: int, present=None) -> np.ndarray:
     """Bytes between images of each level of [B, h, w, 4] tensors (0 where
     present[k] is False), from the level sizes alone."""
@@ -79,24 +64,75 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+class _Plan:
+    """Everything a call for one geometry (device, dtype, B, H, W, levels)
+    needs besides the tensors' addresses, made once per thread: level sizes
+    and shapes, per-image strides, the image structs to fill with addresses,
+    the adjoint's workspace (one per stream: launches on one stream are
+    ordered, so the calls on it may share it)."""
+
+    def __init__(self, device, dtype, B: int, H: int, W: int, levels: int):
+        self.lib = N.load()
+        self.preset = _PRESETS[dtype]
+        self.pipes, self.cmd = _objects(self.preset)
+        self.esz = _ELEMENT_BYTES[dtype]
+        self.sizes = level_sizes(W, H, levels)
+        self.n = len(self.sizes)
+        self.shapes = [(B, h, w, 4) for (w, h) in self.sizes]
+        self.strides = _strides(self.sizes, self.esz)
+        self.strides_ptr = _ptr(self.strides)
+        self.img = _image([0] * self.n, W, H)
+        self.img_ptr = _ptr(self.img)
+        self.adj_img = _image([0] * self.n, W, H)
+        self.adj_img_ptr = _ptr(self.adj_img)
+        self.adj_strides = {}  # present-pattern -> (array, pointer)
+        self.ws_bytes = max(int(self.lib.nvproPyramidAdjointWorkspaceBytes(W, H, self.n)) * B, 16)
+        self.ws = {}  # stream -> workspace tensor
+        self.base_stride = H * W * 4 * self.esz
+
+    def workspace(self, stream: int, device):
+        ws = self.ws.get(stream)
+        if ws is None:
+            ws = self.ws[stream] = torch.empty(self.ws_bytes, dtype=torch.uint8, device=device)
+        return ws
+
+    def adjoint_strides(self, present: tuple):
+        e = self.adj_strides.get(present)
+        if e is None:
+            arr = _strides(self.sizes, self.esz, present)
+            e = self.adj_strides[present] = (arr, _ptr(arr))
+        return e[1]
+
+
+def _plan(device, dtype, B: int, H: int, W: int, levels: int) -> _Plan:
+    """The calling thread's plan for a geometry (a plan holds the thread's
+    command object and image arrays it rewrites per call)."""
+    plans = getattr(_tls, "plans", None)
+    if plans is None:
+        plans = _tls.plans = {}
+    key = (device, dtype, B, H, W, levels)
+    p = plans.get(key)
+    if p is None:
+        p = plans[key] = _Plan(device, dtype, B, H, W, levels)
+    return p
+
+
 def forward_levels(base: torch.Tensor, levels: int = 0) -> list[torch.Tensor]:
     """Levels 1..n-1 of the pyramid of base ([B, H, W, 4]); no autograd.  One
     strided call: every dispatch is one launch over the B images."""
     b4 = base if base.dim() == 4 else base.unsqueeze(0)
     b4 = b4.contiguous()
     B, H, W, _ = b4.shape
-    preset = _PRESETS[b4.dtype]
-    sizes, strides = _geometry(W, H, levels, b4.element_size())
+    device, dtype = b4.device, b4.dtype
+    p = _plan(device, dtype, B, H, W, levels)
     # one tensor per level (views of one buffer would turn in-place changes of
     # a level into autograd errors)
-    outs = [torch.empty((B, h, w, 4), dtype=b4.dtype, device=b4.device) for (w, h) in sizes[1:]]
-    pipes, cmd = _objects(preset)
-    lib = N.load()
-    stream = torch.cuda.current_stream(b4.device).cuda_stream
-    img = _image([b4.data_ptr()] + [o.data_ptr() for o in outs], W, H)
-    N.check(lib.nvproPyramidGenerateStrided(cmd.handle, stream, pipes.struct, _ptr(img), _ptr(strides), B,
-                                            len(sizes)),
-            "nvproPyramidGenerateStrided")
+    outs = [torch.empty(s, dtype=dtype, device=device) for s in p.shapes[1:]]
+    p.img[2:2 + p.n] = [b4.data_ptr()] + [o.data_ptr() for o in outs]
+    stream = torch.cuda.current_stream(device).cuda_stream
+    rc = p.lib.nvproPyramidGenerateStrided(p.cmd.handle, stream, p.pipes.struct, p.img_ptr, p.strides_ptr, B, p.n)
+    if rc:
+        N.check(rc, "nvproPyramidGenerateStrided")
     return outs
 
 
@@ -104,22 +140,19 @@ def adjoint(grads: list, shape, dtype, device, levels: int = 0) -> torch.Tensor:
     """Base gradient for upstream gradients of levels 0..n-1 (entries may be
     None), one strided nvproPyramidAdjoint call for the B images."""
     B, H, W, _ = shape
-    preset = _PRESETS[dtype]
-    sizes = _geometry(W, H, levels, _ELEMENT_BYTES[dtype])[0]
-    lib = N.load()
+    p = _plan(device, dtype, B, H, W, levels)
     stream = torch.cuda.current_stream(device).cuda_stream
-    ws_bytes = lib.nvproPyramidAdjointWorkspaceBytes(W, H, len(sizes)) * B
-    ws = torch.empty(max(ws_bytes, 16), dtype=torch.uint8, device=device)
     # [B, h, w, 4] contiguous as they come from autograd; reshape only what is not
     grads = [g if g is None or (g.dim() == 4 and g.is_contiguous()) else g.reshape(B, *g.shape[-3:]).contiguous()
              for g in grads]
-    out = torch.empty((B, H, W, 4), dtype=dtype, device=device)
-    esz = out.element_size()
-    img = _image([0 if g is None else g.data_ptr() for g in grads], W, H)
-    strides = _strides(sizes, esz, [g is not None for g in grads])
-    N.check(lib.nvproPyramidAdjointStrided(stream, preset, _ptr(img), _ptr(strides), out.data_ptr(), 0,
-                                           H * W * 4 * esz, B, len(sizes), ws.data_ptr(), ws.numel()),
-            "nvproPyramidAdjointStrided")
+    out = torch.empty(p.shapes[0], dtype=dtype, device=device)
+    p.adj_img[2:2 + p.n] = [0 if g is None else g.data_ptr() for g in grads]
+    strides_ptr = p.adjoint_strides(tuple(g is not None for g in grads))
+    ws = p.workspace(stream, device)
+    rc = p.lib.nvproPyramidAdjointStrided(stream, p.preset, p.adj_img_ptr, strides_ptr, out.data_ptr(), 0,
+                                          p.base_stride, B, p.n, ws.data_ptr(), p.ws_bytes)
+    if rc:
+        N.check(rc, "nvproPyramidAdjointStrided")
     return out
 
 
