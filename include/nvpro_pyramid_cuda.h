@@ -121,6 +121,52 @@ NVPRO_PYRAMID_API void nvproPyramidDestroyPipeline(NvproPyramidPipeline pipeline
 /* Bytes per texel of a preset (0 for an unknown preset). */
 NVPRO_PYRAMID_API uint32_t nvproPyramidPresetTexelBytes(NvproPyramidPreset preset);
 
+/* ------------------------------------------------------------------------ */
+/* Custom pipelines: a caller's own texel format and reduction (the          */
+/* reference's customisation macros, nvpro_pyramid.glsl:27-120).  The C++    */
+/* header nvpro_pyramid_cuda.hpp makes them from a device-functor set        */
+/* (nvpro_pyramid::createPipelines<F>); at this level a pipeline is a        */
+/* launcher that runs one recorded dispatch.                                 */
+/* ------------------------------------------------------------------------ */
+
+/* The preset value a custom pipeline reports in its dispatch records. */
+#define NVPRO_PYRAMID_PRESET_CUSTOM 0x100u
+
+/* One level of a dispatch: texel (0, 0) of image 0, row pitch, size, and the
+ * bytes between the images of a strided call (0 for one image). */
+typedef struct NvproPyramidLevelDesc {
+  void*    texels;
+  uint64_t rowPitchBytes;
+  uint32_t width;
+  uint32_t height;
+  uint64_t imageStrideBytes;
+} NvproPyramidLevelDesc;
+
+/* One recorded dispatch, as the reference's shader sees it through its push
+ * constant (inputLevel << 5 | levelCount) and its workgroup count. */
+typedef struct NvproPyramidDispatchDesc {
+  uint32_t isFastPipeline;
+  uint32_t inputLevel;
+  uint32_t levelCount;             /* levels filled: 1..6 (fast), 1..2 (general) */
+  uint32_t imageCount;             /* images of the call (grid z of a strided call) */
+  uint64_t groupCount;             /* workgroups dispatched (0 if any count was 0) */
+  NvproPyramidLevelDesc levels[7]; /* levels inputLevel .. inputLevel + levelCount */
+} NvproPyramidDispatchDesc;
+
+/* Enqueue the kernels of one dispatch on `stream`; return NVPRO_PYRAMID_SUCCESS
+ * or an error code (which nvproPyramidEndCmd returns). */
+typedef NvproPyramidResult (*nvpro_pyramid_launcher_t)(void* userData, NvproPyramidStream stream,
+                                                       const NvproPyramidDispatchDesc* dispatch);
+
+/* A fast or general pipeline whose dispatches run through `launcher` (no
+ * reference counterpart as a function: the reference compiles the caller's
+ * shader into a VkPipeline).  Levels bound with it hold texelBytes bytes per
+ * texel; their addresses and row pitches must be multiples of the largest
+ * power of two dividing texelBytes (at most 16). */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCreateCustomPipeline(
+    uint32_t isFastPipeline, uint32_t texelBytes, nvpro_pyramid_launcher_t launcher, void* userData,
+    NvproPyramidPipeline* pPipeline);
+
 /* NvproPyramidPipelines (nvpro_pyramid_dispatch.hpp:29-35).  `layout` is an
  * opaque caller pointer handed unchanged to the dispatcher callbacks (the
  * VkPipelineLayout slot); pushConstantOffset must be 0 (the 4-byte push

@@ -154,11 +154,21 @@ uint16_t floatToHalf(float f) {
 // --------------------------------------------------------------------------
 // Images in the packed MipmapStorage layout (include/mipmap_storage.hpp:53-76).
 
-enum Preset { kSrgba8 = 1, kRgba32f = 2, kRgba16f = 3 };
+// kRgba16Unorm is no preset of the library: the texel format of the custom
+// functor set the tests compile against nvpro_pyramid_cuda.hpp (RGBA 16-bit
+// unorm, load c / 65535, store uint(clamp(v, 0, 1) * 65535 + 0.5)), which
+// defines REDUCE only, so its REDUCE2 and REDUCE4 are the reference's defaults
+// (nvpro_pyramid.glsl:164-177): REDUCE(0.5, v0, 0.5, v1, 0, v1) and
+// REDUCE2(REDUCE2(v00, v01), REDUCE2(v10, v11)).
+enum Preset { kSrgba8 = 1, kRgba32f = 2, kRgba16f = 3, kRgba16Unorm = 4 };
 
 uint32_t texelBytes(int preset) {
-  return preset == kSrgba8 ? 4 : preset == kRgba32f ? 16 : preset == kRgba16f ? 8 : 0;
+  return preset == kSrgba8 ? 4 : preset == kRgba32f ? 16 : (preset == kRgba16f || preset == kRgba16Unorm) ? 8 : 0;
 }
+
+// The reductions of the run in progress are the reference's defaults derived
+// from REDUCE (kRgba16Unorm) instead of the sRGBA8 preset's own macros.
+thread_local bool t_derivedReductions = false;
 
 struct Image {
   int preset;
@@ -191,6 +201,12 @@ struct Image {
       r.v[3] = t.alpha[p[3]];
     } else if (preset == kRgba32f) {
       std::memcpy(r.v, p, 16);
+    } else if (preset == kRgba16Unorm) {
+      for (int c = 0; c < 4; ++c) {
+        uint16_t u;
+        std::memcpy(&u, p + 2 * c, 2);
+        r.v[c] = (float)u / 65535.0f;
+      }
     } else {
       for (int c = 0; c < 4; ++c) {
         uint16_t hv;
@@ -210,6 +226,13 @@ struct Image {
       p[3] = (uint8_t)alphaEncode(v.v[3]);
     } else if (preset == kRgba32f) {
       std::memcpy(p, v.v, 16);
+    } else if (preset == kRgba16Unorm) {
+      for (int c = 0; c < 4; ++c) {
+        const float x = std::fmin(std::fmax(v.v[c], 0.0f), 1.0f);
+        const float t = x * 65535.0f + 0.5f;  // two roundings (-ffp-contract=off)
+        const uint16_t u = (uint16_t)(uint32_t)t;
+        std::memcpy(p + 2 * c, &u, 2);
+      }
     } else {
       for (int c = 0; c < 4; ++c) {
         uint16_t hv = floatToHalf(v.v[c]);
@@ -233,12 +256,14 @@ Vec4 reduce3(float a0, const Vec4& v0, float a1, const Vec4& v1, float a2, const
 }
 // NVPRO_PYRAMID_REDUCE2: 0.5 * (v0 + v1) (preamble.glsl:35).
 Vec4 reduce2(const Vec4& v0, const Vec4& v1) {
+  if (t_derivedReductions) return reduce3(0.5f, v0, 0.5f, v1, 0.0f, v1);
   Vec4 r;
   for (int c = 0; c < 4; ++c) r.v[c] = 0.5f * (v0.v[c] + v1.v[c]);
   return r;
 }
 // NVPRO_PYRAMID_REDUCE4: 0.25 * ((v00 + v01) + (v10 + v11)) (preamble.glsl:37-38).
 Vec4 reduce4(const Vec4& v00, const Vec4& v01, const Vec4& v10, const Vec4& v11) {
+  if (t_derivedReductions) return reduce2(reduce2(v00, v01), reduce2(v10, v11));
   Vec4 r;
   for (int c = 0; c < 4; ++c) {
     float a = v00.v[c] + v01.v[c];
@@ -700,7 +725,8 @@ int orc_default_schedule(uint32_t w, uint32_t h, uint32_t mipLevels, int hasFast
 }
 
 // Run a dispatch sequence (shader semantics) on a packed image whose level 0
-// is filled.  preset: 1 sRGBA8, 2 RGBA32F, 3 RGBA16F.  isFast: 1 fast
+// is filled.  preset: 1 sRGBA8, 2 RGBA32F, 3 RGBA16F, 4 RGBA 16-bit unorm
+// (the tests' custom functor set).  isFast: 1 fast
 // dispatch, 0 general dispatch, 2 linear blit of one level.  fastShared /
 // generalShared: shared-memory format of the fast / general pipeline
 // (0 FP32, 1 SRGB_SHARED, 2 F16_SHARED; sRGBA8 only).
@@ -711,6 +737,10 @@ int orc_run_ex(int preset, int fastShared, int generalShared, uint32_t w, uint32
   if ((fastShared || generalShared) && preset != kSrgba8) return -4;
   if (mipLevels == 0) mipLevels = fullLevels(w, h);
   Image img(preset, w, h, mipLevels, packed);
+  t_derivedReductions = preset == kRgba16Unorm;
+  struct Reset {
+    ~Reset() { t_derivedReductions = false; }
+  } reset;
   for (int i = 0; i < count; ++i) {
     const uint32_t L = pc[i] >> 5, n = pc[i] & 31u;
     if (n == 0 || L + n >= mipLevels) return -2;

@@ -107,6 +107,8 @@ SIGNATURES = {
     "nvproPyramidLastError": (c_char_p, []),
     "nvproPyramidCreatePipeline": (c_int, [c_int, c_uint32, POINTER(c_void_p)]),
     "nvproPyramidCreatePipelineEx": (c_int, [c_int, c_uint32, c_uint32, POINTER(c_void_p)]),
+    # launcher as a function address (nvpro_pyramid_launcher_t, from a compiled functor set)
+    "nvproPyramidCreateCustomPipeline": (c_int, [c_uint32, c_uint32, c_void_p, c_void_p, POINTER(c_void_p)]),
     "nvproPyramidDebugForceWaitTimeout": (c_int, [c_void_p, c_uint32]),
     "nvproPyramidSpeedOfLightProbe": (c_int, [c_void_p, POINTER(NvproPyramidImage), c_uint32]),
     "nvproPyramidPremultiplyAlpha": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p, c_uint64, c_uint32, c_uint32]),

@@ -51,14 +51,20 @@ uint32_t levelDim(uint32_t base, uint32_t k) {
 
 struct NvproPyramidPipeline_T {
   uint32_t magic;
-  uint32_t preset;
+  uint32_t preset;  // NVPRO_PYRAMID_PRESET_* or NVPRO_PYRAMID_PRESET_CUSTOM
   uint32_t isFast;
   uint32_t configBits;
+  uint32_t texelBytes;
+  nvpro_pyramid_launcher_t launcher;  // custom pipelines
+  void* userData;
 };
 
 struct Record {
   NvproPyramidDispatchRecord info;
   NvproPyramidImage image;
+  uint32_t texelBytes;  // of the bound pipeline
+  nvpro_pyramid_launcher_t launcher;
+  void* userData;
 };
 
 struct NvproPyramidCmd_T {
@@ -110,7 +116,7 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
   const NvproPyramidImage& img = rec.image;
   const uint32_t L = rec.info.pushConstant >> NVPRO_PYRAMID_INPUT_LEVEL_SHIFT;
   const uint32_t n = rec.info.pushConstant & 31u;
-  const uint32_t bpp = presetBytes(rec.info.preset);
+  const uint32_t bpp = rec.texelBytes;
   if (n == 0) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "dispatch with level count 0");
   if (rec.info.isBlit && n != 1) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "a blit fills one level");
   if (rec.info.isFastPipeline ? n > kMaxDispatchLevels : n > 2)
@@ -127,10 +133,12 @@ NvproPyramidResult makeParams(const Record& rec, DispatchParams* out) {
   out->inputLevel = L;
   out->levelCount = n;
   out->groups = (rec.info.groupCountY == 0 || rec.info.groupCountZ == 0) ? 0 : rec.info.groupCountX;
+  out->launcher = reinterpret_cast<void*>(rec.launcher);
+  out->userData = rec.userData;
   out->sharedFmt = (rec.info.configBits & NVPRO_PYRAMID_CONFIG_SRGB_SHARED)  ? kSharedSrgb
                    : (rec.info.configBits & NVPRO_PYRAMID_CONFIG_F16_SHARED) ? kSharedF16
                                                                              : kSharedFp32;
-  const uint32_t align = bpp == 4 ? 4 : bpp == 8 ? 8 : 16;
+  const uint32_t align = std::min(16u, bpp & (0u - bpp));  // largest power of two dividing bpp, at most 16
   for (uint32_t k = 0; k <= n; ++k) {
     const uint32_t lvl = L + k;
     LevelView& v = out->lv[k];
@@ -153,7 +161,8 @@ enum LaunchKind : uint32_t {
   kLaunchTma = 0,      // the TMA fast kernel: dispatch `first`, then `small` small dispatches in its tail
   kLaunchGeneral = 1,  // the general chain: `big` strip stages from `first`, then `small` small dispatches
   kLaunchSmall = 2,    // one CTA: `small` small dispatches from `first`
-  kLaunchPortable = 3  // the portable kernels: dispatch `first`
+  kLaunchPortable = 3,  // the portable kernels: dispatch `first`
+  kLaunchCustom = 4     // a custom pipeline's launcher: dispatch `first`
 };
 struct LaunchPlan {
   uint32_t kind, first, big, small;
@@ -188,7 +197,10 @@ uint32_t planLaunches(const DispatchParams* p, uint32_t n, bool fuse, bool porta
   for (uint32_t i = 0; i < n;) {
     LaunchPlan& l = out[count++];
     l = LaunchPlan{kLaunchPortable, i, 1, 0};
-    if (portableOnly) {
+    if (p[i].launcher) {
+      l.kind = kLaunchCustom;
+      i += 1;
+    } else if (portableOnly) {
       i += 1;
     } else if (smallDispatchSupported(p[i])) {
       l.kind = kLaunchSmall;
@@ -213,6 +225,21 @@ uint32_t planLaunches(const DispatchParams* p, uint32_t n, bool fuse, bool porta
     }
   }
   return count;
+}
+
+// A dispatch of a custom pipeline through its launcher.
+NvproPyramidResult launchCustom(const DispatchParams& p, cudaStream_t stream) {
+  NvproPyramidDispatchDesc d{};
+  d.isFastPipeline = p.isFast;
+  d.inputLevel = p.inputLevel;
+  d.levelCount = p.levelCount;
+  d.imageCount = p.batch;
+  d.groupCount = p.groups;
+  for (uint32_t k = 0; k <= p.levelCount; ++k)
+    d.levels[k] = NvproPyramidLevelDesc{p.lv[k].ptr, p.lv[k].pitch, p.lv[k].w, p.lv[k].h, p.imageStride[k]};
+  const auto fn = reinterpret_cast<nvpro_pyramid_launcher_t>(p.launcher);
+  const NvproPyramidResult r = fn(p.userData, reinterpret_cast<NvproPyramidStream>(stream), &d);
+  return r == NVPRO_PYRAMID_SUCCESS ? r : fail(r, "custom pipeline launcher: %s", nvproPyramidResultString(r));
 }
 
 // Enqueue one planned launch with the given scratch.
@@ -274,8 +301,23 @@ NvproPyramidResult nvproPyramidCreatePipelineEx(NvproPyramidPreset preset, uint3
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "SRGB_SHARED and F16_SHARED are exclusive");
   if ((configBits & kShared) && preset != NVPRO_PYRAMID_PRESET_SRGBA8)
     return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "shared-memory formats exist for the sRGBA8 preset only");
-  auto* p = new (std::nothrow)
-      NvproPyramidPipeline_T{kPipelineMagic, uint32_t(preset), isFastPipeline ? 1u : 0u, configBits};
+  auto* p = new (std::nothrow) NvproPyramidPipeline_T{
+      kPipelineMagic, uint32_t(preset), isFastPipeline ? 1u : 0u, configBits, presetBytes(uint32_t(preset)), nullptr,
+      nullptr};
+  if (!p) return fail(NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY, "host allocation failed");
+  *pPipeline = p;
+  return NVPRO_PYRAMID_SUCCESS;
+}
+
+NvproPyramidResult nvproPyramidCreateCustomPipeline(uint32_t isFastPipeline, uint32_t texelBytes,
+                                                    nvpro_pyramid_launcher_t launcher, void* userData,
+                                                    NvproPyramidPipeline* pPipeline) {
+  if (!pPipeline) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "pPipeline is NULL");
+  *pPipeline = nullptr;
+  if (!launcher || texelBytes == 0 || texelBytes > 256)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "a custom pipeline needs a launcher and 1..256 bytes per texel");
+  auto* p = new (std::nothrow) NvproPyramidPipeline_T{kPipelineMagic, NVPRO_PYRAMID_PRESET_CUSTOM,
+                                                      isFastPipeline ? 1u : 0u, 0u, texelBytes, launcher, userData};
   if (!p) return fail(NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY, "host allocation failed");
   *pPipeline = p;
   return NVPRO_PYRAMID_SUCCESS;
@@ -440,6 +482,9 @@ NvproPyramidResult nvproPyramidCmdDispatch(NvproPyramidCmd cmd, uint32_t gx, uin
   r.info.pipelineBound = cmd->pipelineBoundSinceDispatch;
   r.info.barrierBefore = cmd->barrierSinceDispatch;
   r.image = cmd->image;
+  r.texelBytes = cmd->pipeline->texelBytes;
+  r.launcher = cmd->pipeline->launcher;
+  r.userData = cmd->pipeline->userData;
   DispatchParams probe;
   NvproPyramidResult res = makeParams(r, &probe);
   if (res != NVPRO_PYRAMID_SUCCESS) return cmdFail(cmd, res, "%s", t_lastError.c_str());
@@ -455,6 +500,8 @@ NvproPyramidResult nvproPyramidCmdBlitLevel(NvproPyramidCmd cmd, uint32_t srcLev
   if (!cmd->pipeline) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "blit with no bound pipeline (preset)");
   if (!cmd->imageBound) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_STATE, "blit with no bound image");
   if (srcLevel >= 31) return cmdFail(cmd, NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "source level %u", srcLevel);
+  if (cmd->pipeline->launcher)
+    return cmdFail(cmd, NVPRO_PYRAMID_ERROR_UNSUPPORTED, "blits exist for the built-in presets only");
   Record r;
   std::memset(&r, 0, sizeof r);
   r.info.isFastPipeline = 0;
@@ -465,6 +512,7 @@ NvproPyramidResult nvproPyramidCmdBlitLevel(NvproPyramidCmd cmd, uint32_t srcLev
   r.info.pipelineBound = cmd->pipelineBoundSinceDispatch;
   r.info.barrierBefore = cmd->barrierSinceDispatch;
   r.image = cmd->image;
+  r.texelBytes = cmd->pipeline->texelBytes;
   DispatchParams probe;
   NvproPyramidResult res = makeParams(r, &probe);
   if (res != NVPRO_PYRAMID_SUCCESS) return cmdFail(cmd, res, "%s", t_lastError.c_str());
@@ -521,6 +569,12 @@ NvproPyramidResult nvproPyramidEndCmd(NvproPyramidCmd cmd) {
   std::vector<LaunchPlan> plan(params.size());
   plan.resize(planLaunches(params.data(), uint32_t(params.size()), fuse, portableOnly, plan.data()));
   for (const LaunchPlan& l : plan) {
+    if (l.kind == kLaunchCustom) {
+      const NvproPyramidResult r = launchCustom(params[l.first], cmd->stream);
+      if (r != NVPRO_PYRAMID_SUCCESS) return r;
+      ++cmd->launches;
+      continue;
+    }
     // the command's counters serve every launch: launches are stream-ordered
     // and each leaves its counters at zero
     const uint32_t failCta = (l.kind == kLaunchTma && cmd->debugFailNextTma) ? 0u : ~0u;
@@ -819,6 +873,7 @@ NvproPyramidResult defaultParams(NvproPyramidPreset preset, const NvproPyramidIm
   std::memset(&rec, 0, sizeof rec);
   rec.image = *pImage;
   rec.info.preset = uint32_t(preset);
+  rec.texelBytes = presetBytes(uint32_t(preset));
   rec.info.groupCountY = rec.info.groupCountZ = 1;
   SchedEntry sched[NVPRO_PYRAMID_MAX_LEVELS];
   const uint32_t n = defaultSchedule(w, h, mipLevels, sched);
@@ -1098,8 +1153,7 @@ NvproPyramidResult nvproPyramidGenerateStrided(NvproPyramidCmd cmd, NvproPyramid
   if (count > 65535) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "%u images: at most 65535", count);
   if (count > 1 && !imageStrides) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "imageStrides is NULL");
   if (count > 1 && pImage) {
-    const uint32_t bpp =
-        presetBytes(validPipeline(pipelines.generalPipeline) ? pipelines.generalPipeline->preset : 0);
+    const uint32_t bpp = validPipeline(pipelines.generalPipeline) ? pipelines.generalPipeline->texelBytes : 0;
     for (uint32_t k = 0; k < pImage->levelCount && k < NVPRO_PYRAMID_MAX_LEVELS; ++k)
       if (bpp && imageStrides[k] % bpp)
         return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "image stride of level %u is not a texel multiple", k);

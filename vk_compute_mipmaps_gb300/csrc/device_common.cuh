@@ -10,6 +10,7 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include "../../include/nvpro_pyramid_cuda.hpp"
 #include "internal.h"
 #include "srgb_tables.h"
 
@@ -37,40 +38,12 @@ __device__ __forceinline__ float4 reduce3(float a0, float4 v0, float a1, float4 
   return f4add(f4add(f4scale(a0, v0), f4scale(a1, v1)), f4scale(a2, v2));
 }
 
-// 3-tap weights of the general pipeline (nvpro_pyramid.glsl:582-586, :639-643):
-// n = destination size, i = destination coordinate.
-struct Weights3 {
-  float w0, w1, w2;
-};
-__device__ __forceinline__ Weights3 weights3(uint32_t n, uint32_t i) {
-  const float nf = __uint2float_rn(n);
-  const float rcp = __frcp_rn(__fadd_rn(__fmul_rn(2.0f, nf), 1.0f));
-  Weights3 w;
-  w.w0 = __fmul_rn(rcp, __fsub_rn(nf, __uint2float_rn(i)));
-  w.w1 = __fmul_rn(rcp, nf);
-  w.w2 = __fsub_rn(__fsub_rn(1.0f, w.w0), w.w1);
-  return w;
-}
+// 3-tap weights of the general pipeline (nvpro_pyramid.glsl:582-586, :639-643).
+using nvpro_pyramid::detail::Weights3;
+using nvpro_pyramid::detail::weights3;
 
-// kernelSizeFromInputSize_ (nvpro_pyramid.glsl:557-561).
-__host__ __device__ __forceinline__ uint32_t kernelSize(uint32_t inputSize) {
-  return inputSize == 1 ? 1u : (2u | (inputSize & 1u));
-}
-
-// Reduction order of the fast pipeline for level L+k of an n-level dispatch:
-// true = vertical pairs first, 0.25*((TL+BL)+(TR+BR)); false = horizontal
-// pairs first, 0.25*((TL+TR)+(BL+BR)).  Derived from which operand each
-// REDUCE4 call of nvpro_pyramid.glsl receives: the LOAD_REDUCE4 of level 1
-// (:180-188) and the 2x2 step of 6-level dispatches (:342) pair vertically;
-// the subgroup-shuffle stages (:364-397) pair horizontally; the shared-memory
-// tail (:472-531) pairs vertically.
-__host__ __device__ __forceinline__ bool fastVerticalFirst(uint32_t n, uint32_t k) {
-  if (k == 1) return true;
-  if (n == 6) return k == 2 || k >= 5;
-  if (n >= 4) return k >= 4;
-  return false;
-}
-
+// REDUCE4 of a 2x2 block in the fast pipeline's order for its level
+// (fastVerticalFirst): vertical pairs first, or horizontal pairs first.
 __device__ __forceinline__ float4 fastReduce(bool vertical, float4 tl, float4 tr, float4 bl, float4 br) {
   return vertical ? reduce4(tl, bl, tr, br) : reduce4(tl, tr, bl, br);
 }

@@ -4,7 +4,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/nvpro_pyramid_rules.h"
+
 namespace nvpyr {
+
+using nvpro_pyramid::fastVerticalFirst;
+using nvpro_pyramid::kernelSize;
+using nvpro_pyramid::sharedHandoffLevel;
 
 constexpr uint32_t kMaxDispatchLevels = 6;  // fast pipeline: 1..6 levels (nvpro_pyramid.glsl:221-225)
 // Dispatches whose input level has at most this many texels run on the
@@ -16,15 +22,6 @@ enum Preset : uint32_t { kSrgba8 = 1, kRgba32f = 2, kRgba16f = 3 };
 
 // Shared-memory formats of the sRGBA8 preset (srgba8_mipmap_preamble.glsl:60-108).
 enum SharedFormat : uint32_t { kSharedFp32 = 0, kSharedSrgb = 1, kSharedF16 = 2 };
-
-// The level (relative to the input level) whose values a dispatch of n levels
-// hands on through shared memory, or 0 if none: L+3 for fast dispatches of 4
-// or 5 levels, L+4 for 6 levels (nvpro_pyramid.glsl:440-462), L+1 for
-// two-level general dispatches (:717).
-inline __host__ __device__ uint32_t sharedHandoffLevel(bool isFast, uint32_t n) {
-  if (isFast) return n == 6 ? 4u : n >= 4 ? 3u : 0u;
-  return n == 2 ? 1u : 0u;
-}
 
 inline uint32_t presetBytes(uint32_t preset) {
   return preset == kSrgba8 ? 4u : preset == kRgba32f ? 16u : preset == kRgba16f ? 8u : 0u;
@@ -54,6 +51,10 @@ struct DispatchParams {
   // L+k at lv[k].ptr + i * imageStride[k].
   uint32_t batch = 1;
   uint64_t imageStride[kMaxDispatchLevels + 1] = {};
+  // Custom pipelines (nvproPyramidCreateCustomPipeline): the launcher
+  // (nvpro_pyramid_launcher_t) and its user data; null for the presets.
+  void* launcher = nullptr;
+  void* userData = nullptr;
 };
 
 // Scratch counter slots.
@@ -73,15 +74,9 @@ struct Scratch {
   uint32_t* error() const { return errorFlag ? errorFlag : counters + kCounterError; }
 };
 
-// Workgroups of the reference's fast dispatcher that cover every 2^n tile of a
-// fast dispatch (nvpro_pyramid_dispatch.hpp:234-238: 4096 input samples per
-// group for 6 levels, else 1024).
+// Workgroups that cover every tile of a fast dispatch (nvpro_pyramid::fastGroupsNeeded).
 inline uint64_t fastGroupsNeeded(const DispatchParams& p) {
-  const uint32_t n = p.levelCount;
-  const uint64_t tiles = uint64_t(p.lv[0].w >> n) * (p.lv[0].h >> n);
-  const uint64_t perGroup = (n > 5 ? 4096u : 1024u) >> (2 * n);
-  const uint64_t per = perGroup ? perGroup : 1;
-  return (tiles + per - 1) / per;
+  return nvpro_pyramid::fastGroupsNeeded(p.lv[0].w, p.lv[0].h, p.levelCount);
 }
 
 // True if the dispatch's workgroups cover every texel it can write (the
