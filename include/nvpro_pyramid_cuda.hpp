@@ -198,14 +198,14 @@ constexpr uint32_t kG2Tile = 16;  // two-level general kernel: a 16x16 tile of l
 constexpr uint32_t kG2Win = 2 * kG2Tile + 1;
 
 template <class F>
-constexpr bool checkFunctors() {
+struct FunctorChecks {
   static_assert(sizeof(typename F::Value) <= 32, "NVPRO_PYRAMID_TYPE should be at most 32 bytes");
   static_assert(std::is_trivially_default_constructible<typename F::Value>::value,
                 "Value must be trivially constructible (it lives in shared memory)");
   static_assert(std::is_trivially_default_constructible<typename F::Tables>::value,
                 "Tables must be trivially constructible (it lives in shared memory)");
-  return true;
-}
+  static constexpr bool ok = true;
+};
 
 // ---------------------------------------------------------------------------
 // Fast pipeline (nvpro_pyramid.glsl:209-534), n = 1..6.  Each CTA owns a
@@ -216,7 +216,7 @@ constexpr bool checkFunctors() {
 // teamSizeLog2_, :414-420).
 template <class F>
 __global__ void __launch_bounds__(kThreads) fastKernel(const DispatchArg p) {
-  static_assert(checkFunctors<F>(), "");
+  static_assert(FunctorChecks<F>::ok, "");
   using V = typename F::Value;
   __shared__ typename F::Tables tables;
   __shared__ V bufA[32 * 32];
@@ -313,7 +313,7 @@ __device__ __forceinline__ typename F::Value reduceSample(const F& f, const Load
 // outputs in row-major order define the coverage.
 template <class F>
 __global__ void __launch_bounds__(kThreads) general1Kernel(const DispatchArg p) {
-  static_assert(checkFunctors<F>(), "");
+  static_assert(FunctorChecks<F>::ok, "");
   __shared__ typename F::Tables tables;
   F::initTables(tables, threadIdx.x, blockDim.x);
   __syncthreads();
@@ -350,7 +350,7 @@ __device__ __forceinline__ bool g2CoveredL1(uint32_t x1, uint32_t y1, uint32_t w
 
 template <class F>
 __global__ void __launch_bounds__(kThreads) general2Kernel(const DispatchArg p) {
-  static_assert(checkFunctors<F>(), "");
+  static_assert(FunctorChecks<F>::ok, "");
   using V = typename F::Value;
   __shared__ typename F::Tables tables;
   __shared__ V win[kG2Win * kG2Win];

@@ -15,8 +15,8 @@ ORC_PATH = ORACLE_DIR / "liborc.so"
 REF_CPU_PATH = ORACLE_DIR / "_ref" / "libref_cpu.so"
 REF_DISPATCH_PATH = ORACLE_DIR / "_ref" / "libref_dispatch.so"
 
-BPP = {1: 4, 2: 16, 3: 8}
-DTYPE = {1: np.uint8, 2: np.float32, 3: np.float16}
+BPP = {1: 4, 2: 16, 3: 8, 4: 8}
+DTYPE = {1: np.uint8, 2: np.float32, 3: np.float16, 4: np.uint16}
 
 _orc = None
 
