@@ -10,7 +10,12 @@
 // separates the stages, as the reference's pipeline barriers separate its
 // dispatches (nvpro_pyramid_dispatch.hpp:150-160).  The barrier's wait is
 // bounded: after kWaitLimit polls it sets the error flag and the kernel
-// returns.
+// returns.  The small dispatches after the run (input levels of at most
+// kSmallMaxTexels texels, of either pipeline) are the tail of the launch: the
+// last CTA to finish the strips runs them with the small-dispatch engine
+// (small_engine.cuh); a chain that starts small is one CTA running the engine.
+// A launch without grid barriers (one strip stage or none) is an ordinary
+// programmatic dependent launch, whose table fill overlaps the previous kernel.
 #include <mutex>
 
 #include "general_strip.cuh"
@@ -70,6 +75,11 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) generalChainKernel(const
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint32_t okFlag;
   const Lut L = fillAlignedLut(smem, threadIdx.x, kThreads);
+  // A launch without grid barriers is a programmatic dependent launch: the
+  // table fill above may overlap the end of the previous kernel on the stream;
+  // the first global access waits here for it to complete.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const bool multi = p.stageCount + (p.tailCount ? 1 : 0) > 1;  // uses the scratch counters
   uint32_t gen = 0;
   if (threadIdx.x == 0 && p.stageCount > 1) gen = ldAcquire(p.barrierGen);  // before this CTA's first arrival
@@ -213,7 +223,21 @@ cudaError_t launchGeneralChain(const DispatchParams* p, uint32_t count, const Di
   if (count == 0) grid = 1;
   void* args[] = {&cp};
   const uint32_t fmt = count ? p[0].sharedFmt : kSharedFp32;  // the engine applies each dispatch's own format
-  e = cudaLaunchCooperativeKernel(chainKernel(fmt), dim3(grid), dim3(kThreads), args, kSmemBytes, stream);
+  if (count > 1) {  // grid barriers: every CTA must be resident
+    e = cudaLaunchCooperativeKernel(chainKernel(fmt), dim3(grid), dim3(kThreads), args, kSmemBytes, stream);
+  } else {  // no CTA waits for another: an ordinary launch, programmatic dependent on the previous kernel
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kSmemBytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelExC(&cfg, chainKernel(fmt), args);
+  }
   if (e != cudaSuccess) return e;
   ++*launches;
   return cudaSuccess;

@@ -80,6 +80,19 @@ __device__ __forceinline__ void smallLevel(const uint32_t* inCodes, const float4
                                            const Codec& C, uint32_t tid, uint32_t nthreads) {
   const uint32_t kx = kernelSize(wi), ky = kernelSize(hi);
   const uint32_t r = recip32(wk);
+  // the 3-tap weights with 1 / (2n + 1) computed once per level (weights3's
+  // arithmetic, term by term)
+  const float nfx = __uint2float_rn(wk), nfy = __uint2float_rn(hk);
+  const float rcpx = __frcp_rn(__fadd_rn(__fmul_rn(2.0f, nfx), 1.0f));
+  const float rcpy = __frcp_rn(__fadd_rn(__fmul_rn(2.0f, nfy), 1.0f));
+  auto wts = [](float nf, float rcp, uint32_t i) {
+    Weights3 w;
+    w.w0 = __fmul_rn(rcp, __fsub_rn(nf, __uint2float_rn(i)));
+    w.w1 = __fmul_rn(rcp, nf);
+    w.w2 = __fsub_rn(__fsub_rn(1.0f, w.w0), w.w1);
+    return w;
+  };
+#pragma unroll 2
   for (uint32_t t = tid; t < wk * hk; t += nthreads) {
     const uint32_t y = divBy(t, r, wk), x = t - y * wk;
     float4 v;
@@ -92,7 +105,7 @@ __device__ __forceinline__ void smallLevel(const uint32_t* inCodes, const float4
     } else {
       // kernel size 1 reads row / column 0 only; 2 and 3 their taps
       const uint32_t y1 = ky > 1 ? 2 * y + 1 : 2 * y, y2 = ky > 2 ? 2 * y + 2 : 2 * y;
-      const Weights3 wy = weights3(hk, y);
+      const Weights3 wy = wts(nfy, rcpy, y);
       float4 h[3];
 #pragma unroll
       for (uint32_t c = 0; c < 3; ++c) {
@@ -103,7 +116,7 @@ __device__ __forceinline__ void smallLevel(const uint32_t* inCodes, const float4
         h[c] = ky == 3 ? reduce3(wy.w0, a, wy.w1, b, wy.w2, e) : ky == 2 ? reduce2(a, b) : a;
       }
       if (kx == 3) {
-        const Weights3 wx = weights3(wk, x);
+        const Weights3 wx = wts(nfx, rcpx, x);
         v = reduce3(wx.w0, h[0], wx.w1, h[1], wx.w2, h[2]);
       } else {
         v = kx == 2 ? reduce2(h[0], h[1]) : h[0];
