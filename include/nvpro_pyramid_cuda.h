@@ -511,20 +511,25 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidDebugNoAllocForceWaitTimeout(Nv
 typedef struct NvproPyramidBatch_T* NvproPyramidBatch;
 
 /* Build flags. */
-#define NVPRO_PYRAMID_BATCH_AUTOTUNE 1u /* pick the work-unit size by timing candidates,
-                                           cached per size class of the batch */
+#define NVPRO_PYRAMID_BATCH_AUTOTUNE 1u /* pick the launch's shape (strip band, fast-region rows,
+                                           threads per CTA) by timing candidates, cached per size
+                                           class of the batch in memory and on disk */
 #define NVPRO_PYRAMID_BATCH_GRAPH 2u    /* launches replay a CUDA graph captured at build */
+#define NVPRO_PYRAMID_BATCH_RETUNE 4u   /* with AUTOTUNE: time the candidates even if a cache has
+                                           the size class (and store the new choice) */
 
 typedef struct NvproPyramidBatchInfo {
   uint32_t imageCount;
-  uint32_t phaseCount; /* dispatches of the longest schedule */
-  uint32_t jobCount;   /* dispatches over all images */
-  uint32_t stripBand;  /* rows of level L+2 per general-pipeline work unit */
-  uint64_t unitCount;  /* work units over all phases */
-  uint32_t autotuned;  /* stripBand chosen by the autotuner */
-  uint32_t fromCache;  /* ... from the cache of an earlier build of the same size class */
-  uint32_t graph;      /* launches replay a CUDA graph */
-  uint32_t reserved;
+  uint32_t phaseCount;     /* dispatches of the longest schedule */
+  uint32_t jobCount;       /* dispatches over all images */
+  uint32_t stripBand;      /* rows of level L+2 per general-pipeline work unit */
+  uint64_t unitCount;      /* work units over all phases */
+  uint32_t autotuned;      /* the shape was chosen by the autotuner */
+  uint32_t fromCache;      /* ... from a cache (an earlier build of the same size class) */
+  uint32_t graph;          /* launches replay a CUDA graph */
+  uint32_t fastRegionRows; /* rows of level L per fast-pipeline work unit (64 texels wide) */
+  uint32_t threadsPerCta;  /* 256 or 384 */
+  uint32_t fromDisk;       /* the cached shape came from the cache file of an earlier process */
 } NvproPyramidBatchInfo;
 
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidCreateBatch(NvproPyramidPreset preset, uint32_t flags,
@@ -545,6 +550,16 @@ NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch ba
  * per strip; 0 = the default, or the autotuner's choice with
  * NVPRO_PYRAMID_BATCH_AUTOTUNE) for the following nvproPyramidBatchBuild. */
 NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchSetStripBand(NvproPyramidBatch batch, uint32_t band);
+
+/* Fix any of the launch's shape parameters for the following
+ * nvproPyramidBatchBuild (0 = default, or the autotuner's choice): the strip
+ * band (1..4096), the rows of level L per fast-pipeline region (16, 32 or 64;
+ * at least 2^n for an n-level dispatch) and the threads per CTA (256 or 384).
+ * The shape never changes the bytes written.  The autotuner's cache file is
+ * NVPRO_PYRAMID_CACHE_DIR/batch_tuning.txt (else $XDG_CACHE_HOME/nvpro_pyramid
+ * or $HOME/.cache/nvpro_pyramid), one line per size class and GPU name. */
+NVPRO_PYRAMID_API NvproPyramidResult nvproPyramidBatchSetTuning(NvproPyramidBatch batch, uint32_t stripBand,
+                                                                uint32_t fastRegionRows, uint32_t threadsPerCta);
 
 /* Generate levels 1.. of every image of the batch on `stream` (no
  * allocation, no host synchronisation).  Launches of one batch must not

@@ -1,6 +1,8 @@
 """Batches (nvproPyramidBatch*): one persistent launch for many sRGBA8 images
 of any sizes; the bytes of every image equal a per-image
 nvproPyramidGenerate, and the oracle's for small images."""
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -107,23 +109,80 @@ def test_batch_256_synthetic_equal_per_image(cuda):
     b.device_status()
 
 
-def test_batch_autotune_cached_per_size_class(cuda):
+@pytest.mark.parametrize("band,rows,threads", [(4, 16, 256), (32, 32, 384), (8, 64, 256), (16, 16, 384)])
+def test_batch_shapes_equal_per_image(cuda, band, rows, threads):
+    """Every launch shape the autotuner can choose (strip band, fast-region
+    rows, threads per CTA) writes the bytes of per-image generation."""
     import torch
+    _, chains = P.pack_chains(MIXED, device=cuda)
+    fill_random(chains, 21)
+    refs = per_image_reference(chains)
+    b = P.Batch()
+    b.set_tuning(band, rows, threads)
+    b.build(chains)
+    info = b.info()
+    assert (info["stripBand"], info["fastRegionRows"], info["threadsPerCta"]) == (band, rows, threads)
+    b.launch()
+    torch.cuda.synchronize()
+    check_equal(chains, refs)
+    b.device_status()
+
+
+_SECOND_PROCESS = """
+import json, sys
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[1] + "/tests")
+import torch
+from vk_compute_mipmaps_gb300 import _native as N
+from vk_compute_mipmaps_gb300 import pyramid as P
+from vk_compute_mipmaps_gb300.workloads import batch_sizes
+import test_batch_gpu as T
+_, chains = P.pack_chains(batch_sizes(24, seed=5, hi=1024), device="cuda")
+T.fill_random(chains, 15)
+refs = T.per_image_reference(chains)
+b = P.Batch(N.BATCH_AUTOTUNE)
+b.build(chains)
+b.launch()
+torch.cuda.synchronize()
+T.check_equal(chains, refs)
+print(json.dumps(b.info()))
+"""
+
+
+def test_batch_autotune_cached_per_size_class(cuda, repo_tmp, monkeypatch):
+    """The autotuner times its candidates once per size class; later builds
+    of the class take the cached shape from memory, and a new process takes
+    it from the cache file without timing -- all writing per-image bytes."""
+    import json
+    import subprocess
+    import sys
+
+    import torch
+    monkeypatch.setenv("NVPRO_PYRAMID_CACHE_DIR", str(repo_tmp))
     sizes = batch_sizes(24, seed=5, hi=1024)
     _, chains = P.pack_chains(sizes, device=cuda)
     fill_random(chains, 14)
     refs = per_image_reference(chains)
-    b1 = P.Batch(N.BATCH_AUTOTUNE)
+    b1 = P.Batch(N.BATCH_AUTOTUNE | N.BATCH_RETUNE)
     b1.build(chains)
     i1 = b1.info()
-    assert i1["autotuned"] == 1 and i1["stripBand"] in (4, 8, 16, 32)
+    assert i1["autotuned"] == 1 and i1["fromCache"] == 0
+    assert i1["stripBand"] in (4, 8, 16, 32) and i1["fastRegionRows"] in (16, 32, 64)
+    assert i1["threadsPerCta"] in (256, 384)
     b1.launch()
     torch.cuda.synchronize()
     check_equal(chains, refs)
     b2 = P.Batch(N.BATCH_AUTOTUNE | N.BATCH_GRAPH)
     b2.build(chains)  # same size class: the cached choice, no timing
     i2 = b2.info()
-    assert i2["fromCache"] == 1 and i2["stripBand"] == i1["stripBand"]
+    shape = ("stripBand", "fastRegionRows", "threadsPerCta")
+    assert i2["fromCache"] == 1 and i2["fromDisk"] == 0 and all(i2[k] == i1[k] for k in shape)
+    lines = (repo_tmp / "batch_tuning.txt").read_text().splitlines()
+    assert lines and lines[-1].split()[1:] == [str(i1[k]) for k in shape]
+    res = subprocess.run([sys.executable, "-c", _SECOND_PROCESS, str(Path(__file__).resolve().parents[1])],
+                         capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-3000:]
+    i3 = json.loads(res.stdout.strip().splitlines()[-1])
+    assert i3["fromDisk"] == 1 and i3["fromCache"] == 1 and all(i3[k] == i1[k] for k in shape)
 
 
 def test_batch_empty_and_errors(cuda, native):

@@ -91,12 +91,15 @@ class NvproPyramidBatchInfo(ctypes.Structure):
         ("autotuned", c_uint32),
         ("fromCache", c_uint32),
         ("graph", c_uint32),
-        ("reserved", c_uint32),
+        ("fastRegionRows", c_uint32),
+        ("threadsPerCta", c_uint32),
+        ("fromDisk", c_uint32),
     ]
 
 
 BATCH_AUTOTUNE = 1
 BATCH_GRAPH = 2
+BATCH_RETUNE = 4
 
 # nvpro_pyramid_dispatcher_t
 DISPATCHER = ctypes.CFUNCTYPE(c_uint32, c_void_p, c_void_p, c_uint32, c_void_p, POINTER(NvproPyramidState))
@@ -152,6 +155,7 @@ SIGNATURES = {
     "nvproPyramidDestroyBatch": (None, [c_void_p]),
     "nvproPyramidBatchBuild": (c_int, [c_void_p, c_void_p, POINTER(NvproPyramidImage), c_uint32, c_uint32]),
     "nvproPyramidBatchSetStripBand": (c_int, [c_void_p, c_uint32]),
+    "nvproPyramidBatchSetTuning": (c_int, [c_void_p, c_uint32, c_uint32, c_uint32]),
     "nvproPyramidBatchLaunch": (c_int, [c_void_p, c_void_p]),
     "nvproPyramidBatchGetInfo": (c_int, [c_void_p, POINTER(NvproPyramidBatchInfo)]),
     "nvproPyramidBatchDeviceStatus": (c_int, [c_void_p]),

@@ -8,8 +8,10 @@
 // the tail of the preceding kernel (NVPRO_PYRAMID_CMD_NO_FUSION disables it);
 // the bytes written are the same either way.
 #include <cuda_runtime.h>
+#include <sys/stat.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -1175,13 +1177,24 @@ NvproPyramidResult nvproPyramidGenerateStrided(NvproPyramidCmd cmd, NvproPyramid
 namespace {
 
 constexpr uint32_t kBatchMagic = 0x4E50424Du;  // 'NPBM'
-constexpr uint32_t kBandCandidates[] = {4, 8, 16, 32};
-constexpr uint32_t kDefaultStripBand = 16;
 
-// Autotuner cache: strip band by size class (device, mip levels and the
-// histogram of log2(max side) over the batch, counts rounded to powers of two).
+// The autotuner's candidates per axis (coordinate descent from the default
+// tuple, one axis after the other).  The reference's precedent is the offline
+// sweep of workgroup and tile sizes of extras/general_pipelines/
+// py2_generate_all.py:9-10 and the fixed choice it led to
+// (nvpro_pyramid_dispatch.hpp:254-258).  Levels per dispatch are not an axis:
+// they are the default dispatcher's (nvproPyramidDefaultFastDispatcher<4, 6>),
+// and other values would change the bytes.
+constexpr uint32_t kBandCandidates[] = {4, 8, 16, 32};
+constexpr uint32_t kRowsCandidates[] = {16, 32, 64};
+constexpr uint32_t kWarpsCandidates[] = {8, 12};
+
+// Autotuner cache: the tuple by size class (GPU name, mip levels and the
+// histogram of log2(max side) over the batch, counts rounded to powers of
+// two), in memory and in a text file that later processes read
+// (sizeClassKey, tuneCacheFile).
 std::mutex g_tuneMu;
-std::map<std::string, uint32_t> g_tuneCache;
+std::map<std::string, BatchTuning> g_tuneCache;
 
 std::string sizeClassKey(const NvproPyramidImage* images, uint32_t count, uint32_t mipLevels) {
   uint32_t hist[32] = {};
@@ -1191,8 +1204,12 @@ std::string sizeClassKey(const NvproPyramidImage* images, uint32_t count, uint32
     ++hist[b];
   }
   int dev = 0;
-  cudaGetDevice(&dev);
-  std::string key = std::to_string(dev) + ":" + std::to_string(mipLevels) + ":";
+  cudaDeviceProp prop{};
+  std::string gpu = "gpu";
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) gpu = prop.name;
+  for (char& c : gpu)
+    if (c == ' ' || c == '\t' || c == '\n') c = '_';
+  std::string key = gpu + ":" + std::to_string(mipLevels) + ":";
   for (uint32_t b = 0; b < 32; ++b) {
     uint32_t c = hist[b], r = 0;
     while (c) {
@@ -1202,6 +1219,55 @@ std::string sizeClassKey(const NvproPyramidImage* images, uint32_t count, uint32
     key += char('a' + r);
   }
   return key;
+}
+
+// The cache file: NVPRO_PYRAMID_CACHE_DIR, else $XDG_CACHE_HOME/nvpro_pyramid,
+// else $HOME/.cache/nvpro_pyramid; "" if none can be named.
+std::string tuneCacheFile() {
+  std::string dir;
+  if (const char* d = std::getenv("NVPRO_PYRAMID_CACHE_DIR")) {
+    dir = d;
+  } else if (const char* x = std::getenv("XDG_CACHE_HOME")) {
+    dir = std::string(x) + "/nvpro_pyramid";
+  } else if (const char* h = std::getenv("HOME")) {
+    dir = std::string(h) + "/.cache/nvpro_pyramid";
+  }
+  return dir.empty() ? dir : dir + "/batch_tuning.txt";
+}
+
+// One line per tuned size class: "<key> <band> <rows> <warps>"; the last
+// line of a key wins.  A missing or unreadable file is an empty cache.
+bool readTuneCache(const std::string& key, BatchTuning* t) {
+  const std::string path = tuneCacheFile();
+  if (path.empty()) return false;
+  FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) return false;
+  char line[512];
+  bool found = false;
+  while (std::fgets(line, sizeof line, f)) {
+    char k[400];
+    unsigned band = 0, rows = 0, warps = 0;
+    if (std::sscanf(line, "%399s %u %u %u", k, &band, &rows, &warps) == 4 && key == k && band >= 1 &&
+        band <= 4096 && (rows == 16 || rows == 32 || rows == 64) && (warps == 8 || warps == 12)) {
+      *t = BatchTuning{band, rows, warps};
+      found = true;
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+// Append a tuned size class (best effort: no directory or no permission
+// leaves the in-memory cache only).  One write of one short line.
+void writeTuneCache(const std::string& key, const BatchTuning& t) {
+  const std::string path = tuneCacheFile();
+  if (path.empty()) return;
+  const std::string dir = path.substr(0, path.rfind('/'));
+  mkdir(dir.c_str(), 0755);  // one level; its parent is expected to exist
+  FILE* f = std::fopen(path.c_str(), "a");
+  if (!f) return;
+  std::fprintf(f, "%s %u %u %u\n", key.c_str(), t.stripBand, t.fastRows, t.warps);
+  std::fclose(f);
 }
 
 }  // namespace
@@ -1215,9 +1281,9 @@ struct NvproPyramidBatch_T {
   void* devMem = nullptr;
   uint64_t devBytes = 0;
   uint32_t imageCount = 0;
-  uint32_t stripBand = kDefaultStripBand;
-  uint32_t fixedBand = 0;  // nvproPyramidBatchSetStripBand: overrides default and autotuner
-  uint32_t autotuned = 0, fromCache = 0;
+  BatchTuning tuning;
+  BatchTuning fixed{0, 0, 0};  // nvproPyramidBatchSetTuning: non-zero fields override default and autotuner
+  uint32_t autotuned = 0, fromCache = 0, fromDisk = 0;
   cudaStream_t captureStream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1235,9 +1301,17 @@ struct NvproPyramidBatch_T {
     if (devMem) cudaFree(devMem);
     magic = 0;
   }
-  // plan with `band` and copy it to the device block (grown if needed)
-  cudaError_t planAndUpload(const std::vector<std::vector<DispatchParams>>& imgs, uint32_t band, cudaStream_t s) {
-    cudaError_t e = plan.build(imgs, band);
+  // the tuple with the fixed fields applied
+  BatchTuning withFixed(BatchTuning t) const {
+    if (fixed.stripBand) t.stripBand = fixed.stripBand;
+    if (fixed.fastRows) t.fastRows = fixed.fastRows;
+    if (fixed.warps) t.warps = fixed.warps;
+    return t;
+  }
+  // plan with `tuning` and copy it to the device block (grown if needed)
+  cudaError_t planAndUpload(const std::vector<std::vector<DispatchParams>>& imgs, const BatchTuning& t,
+                            cudaStream_t s) {
+    cudaError_t e = plan.build(imgs, t);
     if (e != cudaSuccess) return e;
     const uint64_t need = plan.deviceBytes();
     if (need > devBytes) {
@@ -1254,7 +1328,58 @@ struct NvproPyramidBatch_T {
       e = cudaMemset(devMem, 0, need);  // the error flag starts clear
       if (e != cudaSuccess) return e;
     }
-    return plan.upload(devMem, s, &dev);
+    e = plan.upload(devMem, s, &dev);
+    dev.warps = t.warps;
+    return e;
+  }
+  // median of five timed launches (after two untimed) of the current plan
+  cudaError_t time(cudaStream_t s, cudaEvent_t* ev, float* ms) {
+    constexpr int kWarm = 2, kTimed = 5;
+    float t[kTimed] = {};
+    uint32_t launches = 0;
+    cudaError_t e = cudaSuccess;
+    for (int it = 0; it < kWarm + kTimed && e == cudaSuccess; ++it) {
+      const bool timed = it >= kWarm;
+      if (timed) e = cudaEventRecord(ev[0], s);
+      if (e == cudaSuccess) e = nvpyr::launchBatch(dev, s, &launches);
+      if (e == cudaSuccess && timed) e = cudaEventRecord(ev[1], s);
+      if (e == cudaSuccess && timed) e = cudaEventSynchronize(ev[1]);
+      if (e == cudaSuccess && timed) e = cudaEventElapsedTime(&t[it - kWarm], ev[0], ev[1]);
+    }
+    std::sort(t, t + kTimed);
+    *ms = t[kTimed / 2];
+    return e;
+  }
+  // coordinate descent over the candidates of the axes that are not fixed
+  cudaError_t autotune(const std::vector<std::vector<DispatchParams>>& imgs, cudaStream_t s, BatchTuning* best) {
+    cudaEvent_t ev[2];
+    cudaError_t e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    BatchTuning cur = withFixed(BatchTuning{});
+    float bestMs = 0;
+    auto tryTuple = [&](const BatchTuning& t) {
+      float ms = 0;
+      if (e == cudaSuccess) e = planAndUpload(imgs, t, s);
+      if (e == cudaSuccess) e = time(s, ev, &ms);
+      if (e == cudaSuccess && (bestMs == 0 || ms < bestMs)) {
+        bestMs = ms;
+        cur = t;
+      }
+    };
+    tryTuple(cur);
+    if (!fixed.stripBand)
+      for (uint32_t b : kBandCandidates)
+        if (b != cur.stripBand) tryTuple(BatchTuning{b, cur.fastRows, cur.warps});
+    if (!fixed.fastRows)
+      for (uint32_t r : kRowsCandidates)
+        if (r != cur.fastRows) tryTuple(BatchTuning{cur.stripBand, r, cur.warps});
+    if (!fixed.warps)
+      for (uint32_t w : kWarpsCandidates)
+        if (w != cur.warps) tryTuple(BatchTuning{cur.stripBand, cur.fastRows, w});
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    *best = cur;
+    return e;
   }
 };
 
@@ -1269,7 +1394,7 @@ NvproPyramidResult nvproPyramidCreateBatch(NvproPyramidPreset preset, uint32_t f
   *pBatch = nullptr;
   if (preset != NVPRO_PYRAMID_PRESET_SRGBA8)
     return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "batches exist for the sRGBA8 preset only");
-  if (flags & ~(NVPRO_PYRAMID_BATCH_AUTOTUNE | NVPRO_PYRAMID_BATCH_GRAPH))
+  if (flags & ~(NVPRO_PYRAMID_BATCH_AUTOTUNE | NVPRO_PYRAMID_BATCH_GRAPH | NVPRO_PYRAMID_BATCH_RETUNE))
     return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "unknown batch flags 0x%x", flags);
   auto* b = new (std::nothrow) NvproPyramidBatch_T;
   if (!b) return fail(NVPRO_PYRAMID_ERROR_OUT_OF_MEMORY, "batch object");
@@ -1300,60 +1425,39 @@ NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch b, NvproPyramidStrea
     imgs[i].assign(params, params + count);
   }
   b->imageCount = imageCount;
-  b->autotuned = b->fromCache = 0;
-  uint32_t band = kDefaultStripBand;
+  b->autotuned = b->fromCache = b->fromDisk = 0;
+  BatchTuning tuning = b->withFixed(BatchTuning{});
   cudaError_t e = cudaSuccess;
-  if (b->fixedBand) {
-    band = b->fixedBand;
-  } else if (b->flags & NVPRO_PYRAMID_BATCH_AUTOTUNE) {
+  const bool allFixed = b->fixed.stripBand && b->fixed.fastRows && b->fixed.warps;
+  if ((b->flags & NVPRO_PYRAMID_BATCH_AUTOTUNE) && !allFixed) {
     const std::string key = sizeClassKey(images, imageCount, mipLevels);
     bool cached = false;
-    {
+    if (!(b->flags & NVPRO_PYRAMID_BATCH_RETUNE)) {
       std::lock_guard<std::mutex> lock(g_tuneMu);
       auto it = g_tuneCache.find(key);
       if (it != g_tuneCache.end()) {
-        band = it->second;
+        tuning = b->withFixed(it->second);
         cached = true;
+      } else if (readTuneCache(key, &tuning)) {
+        g_tuneCache[key] = tuning;
+        tuning = b->withFixed(tuning);
+        cached = true;
+        b->fromDisk = 1;
       }
     }
     if (!cached) {
-      // Time each candidate on `stream` (two warm-up runs, then the median of
-      // five) -- the real work, writing the images' levels.
-      constexpr int kWarm = 2, kTimed = 5;
-      float best = 0;
-      cudaEvent_t ev[2];
-      e = cudaEventCreate(&ev[0]);
-      if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
-      for (uint32_t c : kBandCandidates) {
-        if (e != cudaSuccess) break;
-        e = b->planAndUpload(imgs, c, s);
-        uint32_t launches = 0;
-        float t[kTimed] = {};
-        for (int it = 0; it < kWarm + kTimed && e == cudaSuccess; ++it) {
-          const bool timed = it >= kWarm;
-          if (timed) e = cudaEventRecord(ev[0], s);
-          if (e == cudaSuccess) e = nvpyr::launchBatch(b->dev, s, &launches);
-          if (e == cudaSuccess && timed) e = cudaEventRecord(ev[1], s);
-          if (e == cudaSuccess && timed) e = cudaEventSynchronize(ev[1]);
-          if (e == cudaSuccess && timed) e = cudaEventElapsedTime(&t[it - kWarm], ev[0], ev[1]);
-        }
-        std::sort(t, t + kTimed);
-        if (e == cudaSuccess && (best == 0 || t[kTimed / 2] < best)) {
-          best = t[kTimed / 2];
-          band = c;
-        }
-      }
-      cudaEventDestroy(ev[0]);
-      cudaEventDestroy(ev[1]);
+      // Time the candidates on `stream` -- the real work, writing the images' levels.
+      e = b->autotune(imgs, s, &tuning);
       if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "batch autotune: %s", cudaGetErrorString(e));
       std::lock_guard<std::mutex> lock(g_tuneMu);
-      g_tuneCache[key] = band;
+      g_tuneCache[key] = tuning;
+      writeTuneCache(key, tuning);
     }
     b->autotuned = 1;
     b->fromCache = cached ? 1 : 0;
   }
-  b->stripBand = band;
-  e = b->planAndUpload(imgs, band, s);
+  b->tuning = tuning;
+  e = b->planAndUpload(imgs, tuning, s);
   if (e == cudaErrorInvalidValue)
     return fail(NVPRO_PYRAMID_ERROR_UNSUPPORTED, "a dispatch of the batch is not supported by the batch kernel");
   if (e != cudaSuccess) return fail(NVPRO_PYRAMID_ERROR_CUDA, "batch tables: %s", cudaGetErrorString(e));
@@ -1380,8 +1484,18 @@ NvproPyramidResult nvproPyramidBatchBuild(NvproPyramidBatch b, NvproPyramidStrea
 
 NvproPyramidResult nvproPyramidBatchSetStripBand(NvproPyramidBatch b, uint32_t band) {
   if (!validBatch(b)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid batch object");
-  if (band > 4096) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "strip band %u > 4096", band);
-  b->fixedBand = band;
+  return nvproPyramidBatchSetTuning(b, band, b->fixed.fastRows, b->fixed.warps * 32);
+}
+
+NvproPyramidResult nvproPyramidBatchSetTuning(NvproPyramidBatch b, uint32_t stripBand, uint32_t fastRegionRows,
+                                              uint32_t threadsPerCta) {
+  if (!validBatch(b)) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "invalid batch object");
+  if (stripBand > 4096) return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "strip band %u > 4096", stripBand);
+  if (fastRegionRows != 0 && fastRegionRows != 16 && fastRegionRows != 32 && fastRegionRows != 64)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "fast region rows %u: 16, 32 or 64", fastRegionRows);
+  if (threadsPerCta != 0 && threadsPerCta != 256 && threadsPerCta != 384)
+    return fail(NVPRO_PYRAMID_ERROR_INVALID_ARGUMENT, "threads per CTA %u: 256 or 384", threadsPerCta);
+  b->fixed = BatchTuning{stripBand, fastRegionRows, threadsPerCta / 32};
   return NVPRO_PYRAMID_SUCCESS;
 }
 
@@ -1406,7 +1520,10 @@ NvproPyramidResult nvproPyramidBatchGetInfo(NvproPyramidBatch b, NvproPyramidBat
   info->imageCount = b->imageCount;
   info->phaseCount = b->plan.phaseCount();
   info->jobCount = b->plan.jobCount();
-  info->stripBand = b->stripBand;
+  info->stripBand = b->tuning.stripBand;
+  info->fastRegionRows = b->tuning.fastRows;
+  info->threadsPerCta = b->tuning.warps * 32;
+  info->fromDisk = b->fromDisk;
   info->unitCount = b->plan.unitCount();
   info->autotuned = b->autotuned;
   info->fromCache = b->fromCache;

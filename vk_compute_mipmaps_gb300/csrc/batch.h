@@ -11,6 +11,13 @@
 
 namespace nvpyr {
 
+// The tunable shape of a batch launch (no influence on the bytes written).
+struct BatchTuning {
+  uint32_t stripBand = 16;  // rows of level L+2 per general-pipeline strip unit
+  uint32_t fastRows = 64;   // rows of level L per fast-pipeline region unit (at least 2^n, at most 64)
+  uint32_t warps = 12;      // warps per CTA: 8 or 12
+};
+
 // The plan's tables in device memory (one block, written by upload).
 struct BatchDevice {
   void* device = nullptr;
@@ -19,6 +26,7 @@ struct BatchDevice {
   const uint32_t* phaseUnits = nullptr;
   uint32_t* counters = nullptr;  // unit counters [phases], barrier count, generation, error flag
   uint32_t phaseCount = 0;
+  uint32_t warps = 12;  // CTA size of the launch
   uint64_t countersOffset = 0;
   uint64_t countersBytes = 0;
 };
@@ -31,10 +39,11 @@ class BatchPlan {
   BatchPlan& operator=(const BatchPlan&) = delete;
 
   // Phases and jobs for images[i] = the dispatches of image i's schedule
-  // (sRGBA8, full workgroup coverage).  stripBand: rows of level L+2 per
-  // strip of a two-level general dispatch (one-level: twice as many rows of
-  // level L+1).  cudaErrorInvalidValue if a dispatch is not supported.
-  cudaError_t build(const std::vector<std::vector<DispatchParams>>& images, uint32_t stripBand);
+  // (sRGBA8, full workgroup coverage), with units of the tuning's sizes
+  // (strip band: rows of level L+2 per strip of a two-level general dispatch,
+  // twice as many rows of level L+1 for one level).  cudaErrorInvalidValue if
+  // a dispatch is not supported.
+  cudaError_t build(const std::vector<std::vector<DispatchParams>>& images, const BatchTuning& tuning);
   uint64_t deviceBytes() const;  // upper bound of the device block
   // Copy the tables into `device` (deviceBytes() bytes) and synchronise `stream`.
   cudaError_t upload(void* device, cudaStream_t stream, BatchDevice* out) const;
@@ -53,7 +62,7 @@ class BatchPlan {
 cudaError_t batchDeviceReady();
 
 // Zero the unit counters and barrier words, then launch the batch kernel
-// (cooperative) on `stream`.
+// (cooperative, d.warps warps per CTA) on `stream`.
 cudaError_t launchBatch(const BatchDevice& d, cudaStream_t stream, uint32_t* launches);
 
 }  // namespace nvpyr

@@ -31,13 +31,15 @@
 namespace nvpyr {
 namespace {
 
-constexpr uint32_t kWarps = 12;
-constexpr uint32_t kThreads = 32 * kWarps;
-constexpr uint32_t kRegion = 64;  // fast units: 64x64 texels of level L
+// CTA sizes the autotuner chooses from (WARPS template instances): 8 warps
+// (up to 255 registers per thread) or 12 warps (168).
+constexpr uint32_t kMaxWarps = 12;
+constexpr uint32_t kRegion = 64;  // fast units: 64 texels of level L wide, `rows` high
 constexpr uint32_t kTopBytes = kMaxDispatchLevels * 32 * 16;  // per warp: fast-region rows kept per level
 constexpr uint32_t kJobIndexMax = 1024;  // jobs of a phase whose first units are searched in shared memory
-constexpr uint32_t kSmemBytes = kAlignedLutSmemBytes + kWarps * kTopBytes + kJobIndexMax * 4;
-static_assert(kSmemBytes + 1024 <= 232448, "exceeds the shared memory of a CTA");
+template <uint32_t WARPS>
+constexpr uint32_t kSmemBytesOf = kAlignedLutSmemBytes + WARPS * kTopBytes + kJobIndexMax * 4;
+static_assert(kSmemBytesOf<kMaxWarps> + 1024 <= 232448, "exceeds the shared memory of a CTA");
 constexpr uint32_t kFastGroupRows = 2;  // level-(L+1) rows of a fast region whose level-L rows load together
 
 // One fast dispatch of n levels from level L (nvpro_pyramid.glsl:209-534).
@@ -49,6 +51,7 @@ struct FastJob {
   uint32_t n;
   uint32_t coverW, coverH;  // level L extent covered by whole 2^n tiles
   uint32_t regionsX;
+  uint32_t rows;  // region height: a multiple of 2^n, at most kRegion
 };
 
 // A general dispatch with a one-texel-wide level (kernel size 1 on an axis).
@@ -105,8 +108,8 @@ __device__ __noinline__ void fastRegion(const FastJob& fjob, uint32_t unit, uint
   const uint8_t* const src = f.src;
   uint8_t* const d1 = f.dst[0];
   const uint64_t p1 = f.pitch[0];
-  const uint32_t x0 = (unit % regionsX) * kRegion, y0 = (unit / regionsX) * kRegion;
-  const uint32_t rw = min(kRegion, coverW - x0), rh = min(kRegion, coverH - y0);
+  const uint32_t x0 = (unit % regionsX) * kRegion, y0 = (unit / regionsX) * f.rows;
+  const uint32_t rw = min(kRegion, coverW - x0), rh = min(f.rows, coverH - y0);
   const bool colOk = 2 * lane < rw;
   const uint8_t* base = src + uint64_t(y0) * pitch + uint64_t(x0 + (colOk ? 2 * lane : 0)) * 4;
   const uint32_t rows1 = rh / 2;  // level-(L+1) rows of the region
@@ -228,7 +231,9 @@ __device__ __noinline__ void stripUnit(const Stage& st, uint32_t local, uint32_t
   strip<kSharedFp32>(st, local % st.tilesX, local / st.tilesX, lane, L);
 }
 
-__global__ void __launch_bounds__(kThreads, 1) batchKernel(const __grid_constant__ BatchParams p) {
+template <uint32_t WARPS>
+__global__ void __launch_bounds__(32 * WARPS, 1) batchKernel(const __grid_constant__ BatchParams p) {
+  constexpr uint32_t kWarps = WARPS, kThreads = 32 * WARPS;
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint32_t okFlag;
   const Lut L = fillAlignedLut(smem, threadIdx.x, kThreads);
@@ -272,10 +277,21 @@ __global__ void __launch_bounds__(kThreads, 1) batchKernel(const __grid_constant
 
 struct DeviceState {
   int sms = 0;
-  int ctasPerSm = 0;
 };
 
-cudaError_t deviceState(int* sms, int* ctasPerSm) {
+template <uint32_t WARPS>
+cudaError_t setUp(int dev) {
+  cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(batchKernel<WARPS>),
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytesOf<WARPS>));
+  int ctasPerSm = 0;
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctasPerSm, batchKernel<WARPS>, 32 * WARPS,
+                                                      kSmemBytesOf<WARPS>);
+  if (e == cudaSuccess && ctasPerSm < 1) e = cudaErrorInvalidConfiguration;
+  return e;
+}
+
+cudaError_t deviceState(int* sms) {
   static DeviceState states[64];
   static std::mutex mu;
   int dev = 0;
@@ -289,17 +305,12 @@ cudaError_t deviceState(int* sms, int* ctasPerSm) {
     e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (e != cudaSuccess) return e;
     if (!coop) return cudaErrorNotSupported;
-    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(batchKernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(kSmemBytes));
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.ctasPerSm, batchKernel, kThreads, kSmemBytes);
-    if (e != cudaSuccess) return e;
-    if (d.ctasPerSm < 1) return cudaErrorInvalidConfiguration;
-    e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+    e = setUp<8>(dev);
+    if (e == cudaSuccess) e = setUp<12>(dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
   }
   *sms = d.sms;
-  *ctasPerSm = d.ctasPerSm;
   return cudaSuccess;
 }
 
@@ -330,7 +341,8 @@ uint64_t BatchPlan::deviceBytes() const {
   return t_->jobs.size() * sizeof(BatchJob) + (2 * phases + 1) * 4 + phases * 4 + 4 * 4 + 256;
 }
 
-cudaError_t BatchPlan::build(const std::vector<std::vector<DispatchParams>>& images, uint32_t stripBand) {
+cudaError_t BatchPlan::build(const std::vector<std::vector<DispatchParams>>& images, const BatchTuning& tuning) {
+  const uint32_t stripBand = tuning.stripBand;
   Tables& t = *t_;
   t.jobs.clear();
   t.phaseJobBegin.assign(1, 0);
@@ -363,7 +375,8 @@ cudaError_t BatchPlan::build(const std::vector<std::vector<DispatchParams>>& ima
         j.fast.coverW = cw;
         j.fast.coverH = ch;
         j.fast.regionsX = (cw + kRegion - 1) / kRegion;
-        j.unitCount = j.fast.regionsX * ((ch + kRegion - 1) / kRegion);
+        j.fast.rows = std::min(kRegion, std::max(tuning.fastRows, 1u << n));  // whole 2^n tiles per region
+        j.unitCount = j.fast.regionsX * ((ch + j.fast.rows - 1) / j.fast.rows);
       } else if (generalFastSupported(d)) {
         j.kind = kJobStrip;
         stageGeometry(d, &j.strip);
@@ -438,14 +451,15 @@ cudaError_t BatchPlan::upload(void* device, cudaStream_t stream, BatchDevice* ou
 uint64_t BatchPlan::errorFlagOffset() const { return phaseCount() * 4 + 8; }
 
 cudaError_t batchDeviceReady() {
-  int sms = 0, ctasPerSm = 0;
-  return deviceState(&sms, &ctasPerSm);
+  int sms = 0;
+  return deviceState(&sms);
 }
 
 cudaError_t launchBatch(const BatchDevice& d, cudaStream_t stream, uint32_t* launches) {
   if (d.phaseCount == 0) return cudaSuccess;
-  int sms = 0, ctasPerSm = 0;
-  cudaError_t e = deviceState(&sms, &ctasPerSm);
+  if (d.warps != 8 && d.warps != 12) return cudaErrorInvalidValue;
+  int sms = 0;
+  cudaError_t e = deviceState(&sms);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(d.counters, 0, d.phaseCount * 4 + 8, stream);  // unit counters and barrier count
   if (e != cudaSuccess) return e;
@@ -459,16 +473,16 @@ cudaError_t launchBatch(const BatchDevice& d, cudaStream_t stream, uint32_t* lau
   p.barrierGen = d.counters + d.phaseCount + 1;
   p.errorFlag = d.counters + d.phaseCount + 2;
   cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(uint32_t(sms * std::min(ctasPerSm, 1)));
-  cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = kSmemBytes;
+  cfg.gridDim = dim3(uint32_t(sms));  // one CTA per SM (all resident: the phases' grid barriers)
+  cfg.blockDim = dim3(32 * d.warps);
+  cfg.dynamicSmemBytes = d.warps == 8 ? kSmemBytesOf<8> : kSmemBytesOf<12>;
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  e = cudaLaunchKernelEx(&cfg, batchKernel, p);
+  e = d.warps == 8 ? cudaLaunchKernelEx(&cfg, batchKernel<8>, p) : cudaLaunchKernelEx(&cfg, batchKernel<12>, p);
   if (e != cudaSuccess) return e;
   ++*launches;
   return cudaSuccess;

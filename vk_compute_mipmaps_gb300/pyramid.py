@@ -464,6 +464,11 @@ class Batch:
         """Fix the general-pipeline unit size for the next build (0: default / autotuned)."""
         N.check(self._lib.nvproPyramidBatchSetStripBand(self._h, band), "batch strip band")
 
+    def set_tuning(self, strip_band: int = 0, fast_region_rows: int = 0, threads_per_cta: int = 0) -> None:
+        """Fix shape parameters of the next build (0 = default / autotuned)."""
+        N.check(self._lib.nvproPyramidBatchSetTuning(self._h, strip_band, fast_region_rows, threads_per_cta),
+                "batch tuning")
+
     def launch(self, stream: Optional[int] = None) -> None:
         import torch
         if stream is None:
@@ -473,7 +478,7 @@ class Batch:
     def info(self) -> dict:
         inf = N.NvproPyramidBatchInfo()
         N.check(self._lib.nvproPyramidBatchGetInfo(self._h, ctypes.byref(inf)), "batch info")
-        return {name: getattr(inf, name) for name, _ in N.NvproPyramidBatchInfo._fields_ if name != "reserved"}
+        return {name: getattr(inf, name) for name, _ in N.NvproPyramidBatchInfo._fields_}
 
     def device_status(self) -> None:
         N.check(self._lib.nvproPyramidBatchDeviceStatus(self._h), "batch device status")
