@@ -177,7 +177,9 @@ def test_batch_autotune_cached_per_size_class(cuda, repo_tmp, monkeypatch):
     shape = ("stripBand", "fastRegionRows", "threadsPerCta")
     assert i2["fromCache"] == 1 and i2["fromDisk"] == 0 and all(i2[k] == i1[k] for k in shape)
     lines = (repo_tmp / "batch_tuning.txt").read_text().splitlines()
-    assert lines and lines[-1].split()[1:] == [str(i1[k]) for k in shape]
+    # "<size class> <strip band> <fast-region rows> <warps per CTA>"
+    assert lines and lines[-1].split()[1:] == [str(i1["stripBand"]), str(i1["fastRegionRows"]),
+                                               str(i1["threadsPerCta"] // 32)]
     res = subprocess.run([sys.executable, "-c", _SECOND_PROCESS, str(Path(__file__).resolve().parents[1])],
                          capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stderr[-3000:]
