@@ -283,6 +283,8 @@ def bench_batch(dev, stream, flush, steps, rank=0, world=1):
             "speedup_vs_plain": round(p_us / b_us, 3), "algorithmic_bytes": nbytes,
             "batch_frac_of_hbm_peak": round(nbytes / (b_us * 1e-6) / 1e9 / peak, 4),
             "phases": info["phaseCount"], "jobs": info["jobCount"], "strip_band": info["stripBand"],
+            "fast_region_rows": info["fastRegionRows"], "threads_per_cta": info["threadsPerCta"],
+            "tuning": "autotuned" + (" (cached)" if info["fromCache"] else " (timed at build)"),
             "launches_per_batch": 1, "ranks": world,
             "split": "by image across ranks, max of the ranks' times" if world > 1 else "one GPU"}
 

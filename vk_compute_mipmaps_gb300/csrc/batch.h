@@ -12,10 +12,12 @@
 namespace nvpyr {
 
 // The tunable shape of a batch launch (no influence on the bytes written).
+// The default (measured on the 256-image benchmark batch: 8 warps with up to
+// 255 registers beat 12 with 168 by 1.8x, whatever the unit sizes).
 struct BatchTuning {
-  uint32_t stripBand = 16;  // rows of level L+2 per general-pipeline strip unit
-  uint32_t fastRows = 64;   // rows of level L per fast-pipeline region unit (at least 2^n, at most 64)
-  uint32_t warps = 12;      // warps per CTA: 8 or 12
+  uint32_t stripBand = 8;  // rows of level L+2 per general-pipeline strip unit
+  uint32_t fastRows = 64;  // rows of level L per fast-pipeline region unit (at least 2^n, at most 64)
+  uint32_t warps = 8;      // warps per CTA: 8 or 12
 };
 
 // The plan's tables in device memory (one block, written by upload).
@@ -26,7 +28,7 @@ struct BatchDevice {
   const uint32_t* phaseUnits = nullptr;
   uint32_t* counters = nullptr;  // unit counters [phases], barrier count, generation, error flag
   uint32_t phaseCount = 0;
-  uint32_t warps = 12;  // CTA size of the launch
+  uint32_t warps = 8;  // CTA size of the launch
   uint64_t countersOffset = 0;
   uint64_t countersBytes = 0;
 };
