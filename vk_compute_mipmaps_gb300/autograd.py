@@ -22,6 +22,15 @@ from .pyramid import Cmd, Pipelines, level_sizes
 _PRESETS = {torch.float32: N.PRESET_RGBA32F, torch.float16: N.PRESET_RGBA16F}
 _ELEMENT_BYTES = {torch.float32: 4, torch.float16: 2}
 _tls = threading.local()
+# The current stream's handle by device index without building a Stream
+# object (a few microseconds per call otherwise).
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+
+
+def _stream(device) -> int:
+    if _raw_stream is not None:
+        return _raw_stream(device.index if device.index is not None else torch.cuda.current_device())
+    return torch.cuda.current_stream(device).cuda_stream
 
 
 def _objects(preset: int):
@@ -75,6 +84,7 @@ class _Plan:
         self.lib = N.load()
         self.preset = _PRESETS[dtype]
         self.pipes, self.cmd = _objects(self.preset)
+        self.pipes_struct = self.pipes.struct  # by value in every call
         self.esz = _ELEMENT_BYTES[dtype]
         self.sizes = level_sizes(W, H, levels)
         self.n = len(self.sizes)
@@ -129,8 +139,8 @@ def forward_levels(base: torch.Tensor, levels: int = 0) -> list[torch.Tensor]:
     # a level into autograd errors)
     outs = [torch.empty(s, dtype=dtype, device=device) for s in p.shapes[1:]]
     p.img[2:2 + p.n] = [b4.data_ptr()] + [o.data_ptr() for o in outs]
-    stream = torch.cuda.current_stream(device).cuda_stream
-    rc = p.lib.nvproPyramidGenerateStrided(p.cmd.handle, stream, p.pipes.struct, p.img_ptr, p.strides_ptr, B, p.n)
+    stream = _stream(device)
+    rc = p.lib.nvproPyramidGenerateStrided(p.cmd.handle, stream, p.pipes_struct, p.img_ptr, p.strides_ptr, B, p.n)
     if rc:
         N.check(rc, "nvproPyramidGenerateStrided")
     return outs
@@ -141,7 +151,7 @@ def adjoint(grads: list, shape, dtype, device, levels: int = 0) -> torch.Tensor:
     None), one strided nvproPyramidAdjoint call for the B images."""
     B, H, W, _ = shape
     p = _plan(device, dtype, B, H, W, levels)
-    stream = torch.cuda.current_stream(device).cuda_stream
+    stream = _stream(device)
     # [B, h, w, 4] contiguous as they come from autograd; reshape only what is not
     grads = [g if g is None or (g.dim() == 4 and g.is_contiguous()) else g.reshape(B, *g.shape[-3:]).contiguous()
              for g in grads]

@@ -5,18 +5,17 @@
 // sRGB decode, and the bounded grid barrier between dispatches.
 //
 // A strip is one warp's unit of work: a band of rows of the last level of
-// the dispatch, 15 columns of level L+2 (two levels) or 31 columns of level
-// L+1 (one level).  Lane l owns level-(L+1) column x = x0 + l and loads
-// level-L columns 2x and 2x+1; a three-tap column 2x+2 is lane l+1's first
-// column (shfl.down 1).  The warp walks the band's level-(L+1) rows top to
-// bottom: each row reads two new level-L rows (the third row of a three-tap
-// window is the previous row's last), reduces them vertically per column,
-// then horizontally across lanes (vertical first, as reduceStoreSample_
-// does, :588-651), stores the encoded texel, and keeps the FP32 value for
-// level L+2, which reduces the same way over the lanes' level-(L+1) rows
+// the dispatch, 31 columns of level L+2 (two levels) or 63 columns of level
+// L+1 (one level).  Lane l owns two level-(L+1) columns and loads the four
+// level-L columns under them; a three-tap window's third column is lane
+// l+1's first (shfl.down 1).  The warp walks the band top to bottom, two
+// level-(L+1) rows per step: it reduces the new level-L rows vertically per
+// column, then horizontally (vertical first, as reduceStoreSample_ does,
+// :588-651), stores the encoded texels, and keeps the FP32 values for level
+// L+2, which reduces the same way over the lanes' level-(L+1) values
 // (fillLastTile_ reads FP32 level L+1 from shared memory, :790-820; here it
-// comes from registers).  The level-L rows of the next four level-(L+1) rows
-// are in flight while the current four are reduced.
+// comes from registers).  The level-L rows of the next step are in flight
+// while the current one is reduced.
 //
 // Every texel's value depends only on its inputs and the fixed operation
 // order, so strips overlap by one level-(L+1) column / row where a three-tap
