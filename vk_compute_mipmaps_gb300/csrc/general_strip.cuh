@@ -96,6 +96,15 @@ __device__ __forceinline__ uint32_t ldTexel(const uint8_t* p) {
   return v;
 }
 
+// Steps of level-L rows a strip asks L2 for beyond the rows it holds in
+// registers (prefetch.global.L2: no registers, no completion): the loads of
+// those rows, one step ahead of their use, then hit L2.
+constexpr uint32_t kStripL2Steps = 2;
+
+__device__ __forceinline__ void prefetchL2(const uint8_t* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // Store `v` to `p` if `pred`: a predicated st.global, so the value (an
 // encode every lane computes anyway) is not moved into a divergent branch.
 __device__ __forceinline__ void storeIf(bool pred, uint8_t* p, uint32_t v) {
@@ -202,6 +211,16 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
       p += pitch;
     }
   };
+  // ask L2 for four level-L rows from `row0` (one address per lane: the
+  // lanes' 16-byte column groups cover the strip's span of the row)
+  auto pfRows = [&](uint32_t row0, uint32_t rowEnd) {
+    const uint8_t* p = colA + uint64_t(row0) * pitch;
+#pragma unroll
+    for (uint32_t j = 0; j < 4; ++j) {
+      if (row0 + j < rowEnd) prefetchL2(p);
+      p += pitch;
+    }
+  };
   auto decodeRow = [&](const uint32_t (&r)[4], float4 (&d)[4]) {
 #pragma unroll
     for (uint32_t k = 0; k < 4; ++k) d[k] = decodeAligned(r[k], L);
@@ -246,26 +265,28 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
   // first level-(L+1) row of the steps: rA = yb (+1 when TY1: row yb comes first, alone)
   const uint32_t l0End = 2 * ye + (TY0 ? 1 : 0);  // level-L rows this band reads: [.., l0End)
   float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;  // TY1: level-(L+1) row 2Y of the next level-(L+2) row
-  uint32_t y = yb;
+  // The band's first level-L rows are all requested before any is used: the
+  // carry row (TY0), the two rows of the lone level-(L+1) row (TY1) and the
+  // four rows of the first step, so a short band waits for one round trip
+  // to memory, not three.
+  const uint32_t off = TY0 ? 1 : 0;
+  uint32_t y = yb + (TY1 ? 1 : 0);  // the first step's level-(L+1) row
+  uint32_t r0[4], rT[4][4], bufA[4][4], bufB[4][4];
   if (TY0) {  // level-L row 2yb
-    uint32_t r0[4];
     const uint8_t* p = colA + uint64_t(2 * yb) * pitch;
     r0[0] = ldTexel(p);
     r0[1] = ldTexel(p + d1);
     r0[2] = ldTexel(p + d2);
     r0[3] = ldTexel(p + d3);
-    decodeRow(r0, carry);
   }
-  if (TY1) {  // level-(L+1) row yb alone: the top row of the first level-(L+2) row
-    uint32_t r[4][4];
-    ldRows(2 * yb + (TY0 ? 1 : 0), 2 * yb + (TY0 ? 3 : 2), r);
-    level1Row(y, r[0], r[1], pa, pb);
-    ++y;
-  }
-  // steps of two level-(L+1) rows (y, y + 1); level-L rows from 2y (+1 with TY0)
-  uint32_t bufA[4][4], bufB[4][4];
-  const uint32_t off = TY0 ? 1 : 0;
+  if (TY1) ldRows(2 * yb + off, 2 * yb + off + 2, rT);  // level-L rows of level-(L+1) row yb
   if (y < ye) ldRows(2 * y + off, l0End, bufA);
+  if (TY0) decodeRow(r0, carry);
+  if (TY1) level1Row(yb, rT[0], rT[1], pa, pb);  // the top row of the first level-(L+2) row
+  // steps of two level-(L+1) rows (y, y + 1); level-L rows from 2y (+1 with TY0)
+#pragma unroll
+  for (uint32_t k = 2; k <= kStripL2Steps; ++k)  // the steps before the loop's first prefetch
+    if (y + 2 * k < ye) pfRows(2 * (y + 2 * k) + off, l0End);
   auto step = [&](uint32_t yy, const uint32_t (&r)[4][4]) {
     float4 aA, bA, aB = make_float4(0.f, 0.f, 0.f, 0.f), bB = aB;
     level1Row(yy, r[0], r[1], aA, bA);
@@ -291,13 +312,16 @@ __device__ __forceinline__ void strip(const Stage& st, uint32_t tile, uint32_t b
       storeIf(storeX, dst2 + uint64_t(Y) * pitch2 + uint64_t(X) * 4, encodeTexel(o, L));
     }
   };
+  constexpr uint32_t kPfRows = 2 * (kStripL2Steps + 1);  // level-(L+1) rows ahead of y
   for (;;) {
     if (y >= ye) break;
     if (y + 2 < ye) ldRows(2 * (y + 2) + off, l0End, bufB);
+    if (kStripL2Steps && y + kPfRows < ye) pfRows(2 * (y + kPfRows) + off, l0End);
     step(y, bufA);
     y += 2;
     if (y >= ye) break;
     if (y + 2 < ye) ldRows(2 * (y + 2) + off, l0End, bufA);
+    if (kStripL2Steps && y + kPfRows < ye) pfRows(2 * (y + kPfRows) + off, l0End);
     step(y, bufB);
     y += 2;
   }

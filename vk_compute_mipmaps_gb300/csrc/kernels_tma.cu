@@ -72,6 +72,10 @@ constexpr uint32_t kTileBytes = kTile * kTile * 4;
 constexpr uint32_t kSuspendHintNs = 20000;
 constexpr uint32_t kWaitLimitNs = 1000000000u;
 constexpr uint32_t kWaitPolls = 1u << 22;
+// The timer is read every kPollsPerTimerRead polls (a power of two), not on
+// every poll: waiting warps then take fewer issue slots from the working
+// ones (16384^2 F6 launch 291 -> 287 us).
+constexpr uint32_t kPollsPerTimerRead = 16;
 // Tail counter arrivals: the low 16 bits count CTAs (grids are at most one
 // CTA per SM), a CTA whose wait gave up adds this as well.
 constexpr uint32_t kFailedArrival = 1u << 16;
@@ -136,8 +140,9 @@ __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity), "r"(kSuspendHintNs)
         : "memory");
     if (done) return true;
+    if ((it & (kPollsPerTimerRead - 1)) != kPollsPerTimerRead - 1) continue;
     const uint32_t t = globalTimerLoNs();
-    if (it == 0)
+    if (it == kPollsPerTimerRead - 1)
       t0 = t;
     else if (t - t0 > kWaitLimitNs)
       return false;
