@@ -437,11 +437,12 @@ struct AlignedLutCodec {
 // Fill the aligned tables in `smem` (kAlignedLutSmemBytes of dynamic shared
 // memory) and return the lane's table constants.  Call with every thread of
 // the CTA; a __syncthreads must follow before the first lookup.
+template <uint32_t kBatch = 2>
 __device__ __forceinline__ Lut fillAlignedLut(uint8_t* smem, uint32_t tid, uint32_t nthreads) {
   const uint32_t base = smemAddr(smem);
   const uint32_t decOff = (0x10000u - (base & 0xFFFFu)) & 0xFFFFu;
   const uint32_t thrOff = decOff >= kLutThrBytes ? 0u : decOff + kLutDecodeBytes;
-  fillLut(reinterpret_cast<float*>(smem + decOff), reinterpret_cast<float*>(smem + thrOff), tid, nthreads);
+  fillLut<kBatch>(reinterpret_cast<float*>(smem + decOff), reinterpret_cast<float*>(smem + thrOff), tid, nthreads);
   Lut L = makeLutAt(base + decOff, base + thrOff, tid & 31);
   L.laneWord |= (base + decOff) & 0xFFFF0000u;  // table bytes 2-3 for decodeAligned
   return L;

@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(32 * WARPS, 1) batchKernel(const __grid_consta
   constexpr uint32_t kWarps = WARPS, kThreads = 32 * WARPS;
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ uint32_t okFlag;
-  const Lut L = fillAlignedLut(smem, threadIdx.x, kThreads);
+  const Lut L = fillAlignedLut<(768 + kThreads - 1) / kThreads>(smem, threadIdx.x, kThreads);
   uint32_t gen = 0;
   if (threadIdx.x == 0 && p.phaseCount > 1) gen = ldAcquire(p.barrierGen);  // before this CTA's first arrival
   __syncthreads();

@@ -92,7 +92,10 @@ __device__ __forceinline__ void smallLevel(const uint32_t* inCodes, const float4
     w.w2 = __fsub_rn(__fsub_rn(1.0f, w.w0), w.w1);
     return w;
   };
-#pragma unroll 2
+  // Not unrolled: the engine runs once per launch in one CTA, where the
+  // shorter code is worth more than the overlap of two texels (measured:
+  // 4096^2 chain 43.4 -> 42.2 us, 2560x1440 42.1 -> 39.3 us per launch).
+#pragma unroll 1
   for (uint32_t t = tid; t < wk * hk; t += nthreads) {
     const uint32_t y = divBy(t, r, wk), x = t - y * wk;
     float4 v;

@@ -56,30 +56,35 @@ static __device__ const uint32_t g_srgbTables[3][256] = {
     {NVPYR_SRGB_DECODE_BITS}, {NVPYR_ALPHA_DECODE_BITS}, {NVPYR_SRGB_ENCODE_THRESHOLD_BITS}};
 
 // Fill the replicated tables: decode rows of 256 B (32 copies of decode[c],
-// then 32 of alpha[c]) and threshold rows of 128 B (32 copies).  Warp w
-// fills the rows of codes w, w + nwarps, ...; it loads the table entries of
-// eight codes (the same address across the warp) before storing their rows,
-// lane l writing copy l of each (conflict-free).
+// then 32 of alpha[c]) and threshold rows of 128 B (32 copies).  Each thread
+// takes whole table entries (e = tid, tid + nthreads, ...): it loads up to
+// kBatch before storing any, so with kBatch * nthreads >= 768 the whole fill
+// waits for one round trip to memory, then writes each entry's 32 copies as eight 16-byte stores, lane l
+// starting at 16-byte chunk l % 8 of the row so that a warp's stores spread
+// over all banks (four lanes per chunk: the four wavefronts a 16-byte store
+// of a warp takes anyway).
+template <uint32_t kBatch = 2>
 __device__ __forceinline__ void fillLut(float* dec, float* thr, uint32_t tid, uint32_t nthreads) {
-  constexpr uint32_t kBatch = 8;
-  const uint32_t warp = tid >> 5, l = tid & 31, nwarps = nthreads >> 5;
-  for (uint32_t c0 = warp; c0 < 256; c0 += kBatch * nwarps) {
-    uint32_t d[kBatch], a[kBatch], t[kBatch];
+  constexpr uint32_t kEntries = 3 * 256;
+  const uint32_t rot = tid & 7;
+  for (uint32_t e0 = tid; e0 < kEntries; e0 += kBatch * nthreads) {
+    uint32_t v[kBatch];
 #pragma unroll
     for (uint32_t b = 0; b < kBatch; ++b) {
-      const uint32_t code = min(c0 + b * nwarps, 255u);
-      d[b] = __ldg(&g_srgbTables[0][code]);
-      a[b] = __ldg(&g_srgbTables[1][code]);
-      t[b] = __ldg(&g_srgbTables[2][code]);
+      const uint32_t e = min(e0 + b * nthreads, kEntries - 1);
+      v[b] = __ldg(&g_srgbTables[e >> 8][e & 255]);
     }
 #pragma unroll
     for (uint32_t b = 0; b < kBatch; ++b) {
-      const uint32_t code = c0 + b * nwarps;
-      if (code < 256) {
-        dec[code * 64 + l] = __uint_as_float(d[b]);
-        dec[code * 64 + 32 + l] = __uint_as_float(a[b]);
-        if (code < kThrRows) thr[code * 32 + l] = __uint_as_float(t[b]);
-      }
+      const uint32_t e = e0 + b * nthreads, table = e >> 8, code = e & 255;
+      if (e >= kEntries || (table == 2 && code >= kThrRows)) continue;
+      // the entry's 32 copies: decode row c words 0..31 (table 0) or 32..63
+      // (table 1), threshold row c words 0..31 (table 2)
+      float4* const row = reinterpret_cast<float4*>(table == 2 ? thr + code * 32 : dec + code * 64 + table * 32);
+      const float f = __uint_as_float(v[b]);
+      const float4 q = make_float4(f, f, f, f);
+#pragma unroll
+      for (uint32_t j = 0; j < 8; ++j) row[(j + rot) & 7] = q;
     }
   }
 }
