@@ -41,6 +41,9 @@ template <uint32_t WARPS>
 constexpr uint32_t kSmemBytesOf = kAlignedLutSmemBytes + WARPS * kTopBytes + kJobIndexMax * 4;
 static_assert(kSmemBytesOf<kMaxWarps> + 1024 <= 232448, "exceeds the shared memory of a CTA");
 constexpr uint32_t kFastGroupRows = 2;  // level-(L+1) rows of a fast region whose level-L rows load together
+// Groups of rows a fast region asks L2 for beyond the group it holds in
+// registers (prefetch.global.L2, as the strips do).
+constexpr uint32_t kFastL2Groups = 2;
 
 // One fast dispatch of n levels from level L (nvpro_pyramid.glsl:209-534).
 struct FastJob {
@@ -128,6 +131,18 @@ __device__ __noinline__ void fastRegion(const FastJob& fjob, uint32_t unit, uint
     }
   };
 
+  auto pfGroup = [&](uint32_t r0) {  // ask L2 for the level-L rows of group r0
+    const uint8_t* row = base + uint64_t(2 * r0) * pitch;
+#pragma unroll
+    for (uint32_t j = 0; j < kFastGroupRows; ++j) {
+      if (r0 + j < rows1) {
+        prefetchL2(row);
+        prefetchL2(row + pitch);
+      }
+      row += 2 * pitch;
+    }
+  };
+
   // top[32 k + lane]: level k's row kept from its last even step (the
   // warp's slice of shared memory)
   auto process = [&](uint32_t r0, const uint32_t (&raw)[kFastGroupRows][4]) {
@@ -160,12 +175,17 @@ __device__ __noinline__ void fastRegion(const FastJob& fjob, uint32_t unit, uint
 
   uint32_t bufA[kFastGroupRows][4], bufB[kFastGroupRows][4];
   ldGroup(0, bufA);
+  constexpr uint32_t kPf = kFastGroupRows * (kFastL2Groups + 1);  // rows ahead of r0 asked of L2
+#pragma unroll
+  for (uint32_t g = 2; g <= kFastL2Groups; ++g) pfGroup(g * kFastGroupRows);
   for (uint32_t r0 = 0;;) {
     if (r0 + kFastGroupRows < rows1) ldGroup(r0 + kFastGroupRows, bufB);
+    if (kFastL2Groups && r0 + kPf < rows1) pfGroup(r0 + kPf);
     process(r0, bufA);
     r0 += kFastGroupRows;
     if (r0 >= rows1) break;
     if (r0 + kFastGroupRows < rows1) ldGroup(r0 + kFastGroupRows, bufA);
+    if (kFastL2Groups && r0 + kPf < rows1) pfGroup(r0 + kPf);
     process(r0, bufB);
     r0 += kFastGroupRows;
     if (r0 >= rows1) break;
