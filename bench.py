@@ -622,10 +622,7 @@ def run_ours(args, rank, world):
         "vs_baseline": None,
         "dtype": "u8",
         "data": "synthetic: uniform random bytes (torch.Generator seed 1234)",
-        "config": {"workload": f"sRGBA8 {w}x{h} full chain, reference dispatch schedule",
-                   "image": f"{w}x{h}", "preset": "srgba8", "levels": levels,
-                   "l2": "inputs larger than L2 (1 GiB base level)",
-                   "parallelism": f"replicas x{world}"},
+        "config": headline_config(w, h, levels, world),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                      "algorithmic_bytes_per_launch": kbytes, "launch_us": round(k_ms * 1e3, 2),
@@ -638,6 +635,14 @@ def run_ours(args, rank, world):
     }
     if rank == 0:
         print(json.dumps(line))
+
+
+def headline_config(w, h, levels, world):
+    """The `config` of the bench line, the same for both arms."""
+    return {"workload": f"sRGBA8 {w}x{h} full chain, reference dispatch schedule",
+            "image": f"{w}x{h}", "preset": "srgba8", "levels": levels,
+            "l2": "inputs larger than L2 (1 GiB base level)",
+            "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args, rank, world):
@@ -668,8 +673,7 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "u8",
         "data": "synthetic: uniform random bytes",
-        "config": {"workload": "sRGBA8 16384x16384 full 15-level chain", "image": "16384x16384",
-                   "preset": "srgba8", "levels": 15},
+        "config": headline_config(*HEADLINE, 15, world),
         "cpu_baseline": {"value": round(v, 1), "unit": "us", "cores": threads, "kind": "port",
                          "sample": sample + "; cpuGenerateMipmaps_sRGBA restated (oracle/pyr_oracle.cpp), "
                                             "bit-exact to the reference build"},
