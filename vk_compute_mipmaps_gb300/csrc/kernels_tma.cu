@@ -76,6 +76,10 @@ constexpr uint32_t kWaitPolls = 1u << 22;
 // every poll: waiting warps then take fewer issue slots from the working
 // ones (16384^2 F6 launch 291 -> 287 us).
 constexpr uint32_t kPollsPerTimerRead = 16;
+// The producer warps' waits (buffer empty, exchange full) are off the
+// consumers' critical path: between their polls they sleep, leaving the issue
+// slots to the consumer warps.
+constexpr uint32_t kProducerSleepNs = 256;
 // Tail counter arrivals: the low 16 bits count CTAs (grids are at most one
 // CTA per SM), a CTA whose wait gave up adds this as well.
 constexpr uint32_t kFailedArrival = 1u << 16;
@@ -130,6 +134,9 @@ __device__ __forceinline__ uint32_t globalTimerLoNs() {
   return t;
 }
 
+// SLEEP_NS: after a poll that found the phase incomplete, the warp sleeps
+// this long before the next (0: none).
+template <uint32_t SLEEP_NS = 0>
 __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
   uint32_t t0 = 0;
   for (uint32_t it = 0; it < kWaitPolls; ++it) {
@@ -140,6 +147,7 @@ __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity), "r"(kSuspendHintNs)
         : "memory");
     if (done) return true;
+    if (SLEEP_NS) __nanosleep(SLEEP_NS);
     if ((it & (kPollsPerTimerRead - 1)) != kPollsPerTimerRead - 1) continue;
     const uint32_t t = globalTimerLoNs();
     if (it == kPollsPerTimerRead - 1)
@@ -378,14 +386,14 @@ __device__ __forceinline__ bool producerLoop(const FusedStage& st, const CUtenso
   for (uint32_t iter = 0; cur.ry < st.regionsY; ++iter, cur.next(), ahead.next()) {
     const uint32_t s = iter & 1, parity = (iter >> 1) & 1;
     if (ahead.ry < st.regionsY) {
-      if (!mbarWait(G.empty0 + 8 * s, parity)) return false;
+      if (!mbarWait<kProducerSleepNs>(G.empty0 + 8 * s, parity)) return false;
       if (lane == 0) {
         tmaLoadRegion(G.stage0 + s * kTileBytes, map, ahead.rx * kTile, ahead.ry * kTile, G.full0 + 8 * s);
         ++G.issued[s];
       }
     }
     if (N >= 5) {
-      if (!mbarWait(G.xfull0 + 8 * s, parity)) return false;
+      if (!mbarWait<kProducerSleepNs>(G.xfull0 + 8 * s, parity)) return false;
       const uint32_t x0 = cur.rx * kTile, y0 = cur.ry * kTile;
       if (x0 + kTile > st.coverW || y0 + kTile > st.coverH)
         finishTop<N, true>(st, x0, y0, G.xchg + s * 16, lane, L);
