@@ -54,12 +54,12 @@ struct Stage {
 };
 
 // REDUCE / REDUCE2 (srgba8_mipmap_preamble.glsl:24-38), equal to reduce3() /
-// reduce2(): products on packed pairs (__fmul2_rn).  The sums of REDUCE must
-// stay scalar: __fadd_rn is never merged into a multiply-add, while packed
-// adds next to packed multiplies were seen fused (a fused w0*v0 + w1*v1
-// changes encoded bytes).  REDUCE2's add may be packed: its operands are
-// decoded values, sums, or exact halvings (0.5 * x), so a fused and an
-// unfused result are the same.
+// reduce2(): products on packed pairs (__fmul2_rn).  The sums of REDUCE stay
+// scalar (__fadd_rn): with packed adds (__fadd2_rn) after the packed products
+// one alpha byte of a 255x256 chain came out one off -- also with contraction
+// disabled (-fmad=false), so not a fused multiply-add.  REDUCE2's add may be
+// packed: its operands are decoded values, sums, or exact halvings
+// (0.5 * x), and the parity tests hold for it.
 __device__ __forceinline__ float4 mul4p(float s, float4 a) {
   const float2 lo = __fmul2_rn(make_float2(s, s), make_float2(a.x, a.y));
   const float2 hi = __fmul2_rn(make_float2(s, s), make_float2(a.z, a.w));
