@@ -56,8 +56,8 @@ struct Stage {
 // REDUCE / REDUCE2 (srgba8_mipmap_preamble.glsl:24-38), equal to reduce3() /
 // reduce2(): products on packed pairs (__fmul2_rn).  The sums of REDUCE stay
 // scalar (__fadd_rn): with packed adds (__fadd2_rn) after the packed products
-// one alpha byte of a 255x256 chain came out one off -- also with contraction
-// disabled (-fmad=false), so not a fused multiply-add.  REDUCE2's add may be
+// one alpha byte of a 255x256 chain came out one off, also when compiled with
+// -fmad=false.  REDUCE2's add may be
 // packed: its operands are decoded values, sums, or exact halvings
 // (0.5 * x), and the parity tests hold for it.
 __device__ __forceinline__ float4 mul4p(float s, float4 a) {
