@@ -103,6 +103,12 @@ def test_bench_gpus_flag_launches_ranks():
     lines = [json.loads(ln) for ln in res.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1, res.stdout
     assert lines[0]["n_gpus"] == 2 and lines[0]["impl"] == "reference"
+    # the reference arm reports the GPU arm's workload: same metric and config
+    sys.path.insert(0, str(root))
+    import bench
+    assert lines[0]["metric"] == f"srgba8_{bench.HEADLINE[0]}x{bench.HEADLINE[1]}_full_chain_us"
+    assert lines[0]["config"] == bench.headline_config(*bench.HEADLINE, 15, 2)
+    assert lines[0]["higher_is_better"] is False and lines[0]["unit"] == "us"
 
 
 def test_batch_workload_is_seeded_and_mixed():
